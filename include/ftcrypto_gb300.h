@@ -1,0 +1,75 @@
+/*
+ * ftcrypto_gb300.h — extensions of the ftcrypto.h interface provided by
+ * libftcrypto_gb300.  None of these replaces a reference function; they add
+ * the ciphertext-level and device-pointer entry points that the batched and
+ * serving forms use, and never change the behaviour of ftcrypto.h calls.
+ */
+#ifndef FTCRYPTO_GB300_H
+#define FTCRYPTO_GB300_H
+
+#include "ftcrypto.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error code of the most recent call that has no return value (ft_scale,
+ * ft_neg, ft_index). */
+ft_error ftx_last_error(void);
+
+/* The library's CUDA stream (a cudaStream_t) on which every call runs. */
+void *ftx_stream(void);
+
+/* Waits for all work queued on the library's stream. */
+ft_error ftx_synchronize(void);
+
+/* Device address of the array's storage: 8 planes of 16-byte words, plane
+ * k at planes + k * stride * 16 bytes; point i uses word i of every plane
+ * (X, Y, Z, T, each as two 16-byte words, little-endian, below 2^256 and
+ * congruent to the coordinate mod 2^255-19). */
+ft_error ftx_array_device_view(const_ft_ge25519_array array, void **planes, size_t *stride);
+
+/* 128 bytes per point: X, Y, Z, T as 32-byte little-endian integers (the
+ * library's exact internal values; lossless and cheap). */
+ft_error ftx_array_to_packed(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array array);
+ft_error ftx_array_from_packed(ft_ge25519_array *array, const uint8_t *mem, size_t n_bytes);
+
+/* ft_mul with the n 32-byte scalars already in device memory. */
+ft_error ftx_mul_device(ft_ge25519_array array, const uint8_t *d_scalars, size_t n_scalars);
+
+/* ElGamal encryption of n plaintexts under the public key pk (a folded
+ * 32-byte point): c1[i] = r_i * B, c2[i] = m_i * B + r_i * PK, constant
+ * time in r_i and m_i.  Every m_i must be below 2^plaintext_bits
+ * (1 <= plaintext_bits <= 64; FT_ERR_BAD_SIZE otherwise); r is n 32-byte
+ * scalars.  The points equal the reference's composition
+ * ft_array_from_scalars(r), ft_array_init_point(pk) + ft_mul(r),
+ * ft_array_from_small_scalars(m) + ft_add.  FT_ERR_INVALID_POINT if pk does
+ * not decode. */
+ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *pk, const uint64_t *m,
+                     const uint8_t *r, size_t n, unsigned plaintext_bits);
+
+/* ftx_encrypt into existing arrays of length n, with m and r already in
+ * device memory (m_i < 2^plaintext_bits is not checked). */
+ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint64_t *d_m,
+                            const uint8_t *d_r, size_t n, unsigned plaintext_bits);
+
+/* Segmented sum over CSR offsets: out is a new array of nseg points with
+ * out[s] = sum of src[offsets[s] .. offsets[s+1]) (the identity for an empty
+ * segment).  offsets has nseg + 1 int32 entries, non-decreasing, from 0 to
+ * length(src); FT_ERR_BAD_SIZE otherwise. */
+ft_error ftx_segmented_sum_csr(ft_ge25519_array *out, const int32_t *offsets, size_t nseg,
+                               const_ft_ge25519_array src);
+
+/* The same with offsets in device memory, into an existing array of length
+ * nseg (offsets are trusted). */
+ft_error ftx_segmented_sum_csr_device(ft_ge25519_array out, const int32_t *d_offsets, size_t nseg,
+                                      const_ft_ge25519_array src);
+
+/* out[out_idx] = sum of src, leaving src unchanged. */
+ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_array src);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,17 @@
+"""libftcrypto_gb300 — libftcrypto's batched additively homomorphic ElGamal
+over Ed25519, implemented as hand-written CUDA kernels for NVIDIA GB300
+(sm_103a) behind the reference's ftcrypto.h C ABI (libftcrypto.so).
+
+    from libftcrypto_gb300 import Array, encrypt
+    a = Array.from_small_scalars([1, 2, 3])
+    a.add(a)
+    a.to_bytes_folded()
+
+The C library is the product; this package builds it (build.py), binds it
+(_lib.py) and mirrors its interface in Python (api.py).
+"""
+from .api import (AFFINE, EXTENDED, FOLDED, PACKED, Array, FtError, check, device_memory,  # noqa: F401
+                  encrypt, encrypt_device, error_str, init, segmented_sum_csr, segmented_sum_csr_device,
+                  stream_handle, synchronize)
+from .build import LIB as LIB_PATH  # noqa: F401
+from .build import build  # noqa: F401

@@ -1,0 +1,330 @@
+// fe.cuh — arithmetic in GF(2^255 - 19) for sm_103a.
+//
+// Representation: 8 x 32-bit little-endian limbs holding an integer below
+// 2^256 that is congruent to the field element ("loosely reduced"; values in
+// [p, 2^256) are allowed).  This is the radix that maps onto the 32-bit
+// IMAD / carry-chain datapath: a product is an 8 x 8 operand-scanning
+// schoolbook in mad.lo/madc.hi chains, folded with 2^256 = 38 (mod p).
+// The reference's 10 x 25.5-bit signed limbs (sodium_fe.cu:30) need 100
+// 32x32->64 products per multiplication against 64 here.
+//
+// Canonical reduction and the inversion / square-root addition chains follow
+// fe25519_reduce (sodium_fe.cu:168-241), fe25519_invert (:1352-1408) and
+// fe25519_pow22523 (:1410-1463) of the reference.
+#pragma once
+#ifdef FT_HOST_EMULATION
+#include FT_HOST_EMULATION
+#else
+#include "ptx.cuh"
+#endif
+
+struct fe {
+    uint32_t v[8];
+};
+
+FT_DEV void fe_0(fe &h)
+{
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h.v[k] = 0;
+}
+
+FT_DEV void fe_1(fe &h)
+{
+    fe_0(h);
+    h.v[0] = 1;
+}
+
+FT_DEV fe fe_const(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                   uint32_t a4, uint32_t a5, uint32_t a6, uint32_t a7)
+{
+    fe r;
+    r.v[0] = a0; r.v[1] = a1; r.v[2] = a2; r.v[3] = a3;
+    r.v[4] = a4; r.v[5] = a5; r.v[6] = a6; r.v[7] = a7;
+    return r;
+}
+
+// d = -121665/121666, 2d and sqrt(-1) (the constants of fe_constants.h)
+FT_DEV fe fe_d() { return fe_const(0x135978a3u, 0x75eb4dcau, 0x4141d8abu, 0x00700a4du, 0x7779e898u, 0x8cc74079u, 0x2b6ffe73u, 0x52036ceeu); }
+FT_DEV fe fe_d2() { return fe_const(0x26b2f159u, 0xebd69b94u, 0x8283b156u, 0x00e0149au, 0xeef3d130u, 0x198e80f2u, 0x56dffce7u, 0x2406d9dcu); }
+FT_DEV fe fe_sqrtm1() { return fe_const(0x4a0ea0b0u, 0xc4ee1b27u, 0xad2fe478u, 0x2f431806u, 0x3dfbd7a7u, 0x2b4d0099u, 0x4fc1df0bu, 0x2b832480u); }
+
+// h = a + b  (h < 2^256; a carry out of bit 256 is repaid as +38)
+FT_DEV void fe_add(fe &h, const fe &a, const fe &b)
+{
+    uint32_t r[8];
+    r[0] = add_cc(a.v[0], b.v[0]);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r[k] = addc_cc(a.v[k], b.v[k]);
+    uint32_t c = addc(0u, 0u);
+    r[0] = mad_lo_cc(c, 38u, r[0]);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r[k] = addc_cc(r[k], 0u);
+    c = addc(0u, 0u);
+    // r < 38 whenever c == 1, so this cannot carry
+    r[0] += 38u * c;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h.v[k] = r[k];
+}
+
+// h = a - b  (a borrow of 2^256 is repaid as -38)
+FT_DEV void fe_sub(fe &h, const fe &a, const fe &b)
+{
+    uint32_t r[8];
+    r[0] = sub_cc(a.v[0], b.v[0]);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r[k] = subc_cc(a.v[k], b.v[k]);
+    uint32_t bw = subc(0u, 0u); // 0 or 0xffffffff
+    r[0] = sub_cc(r[0], bw & 38u);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r[k] = subc_cc(r[k], 0u);
+    bw = subc(0u, 0u);
+    // r >= 2^256 - 38 whenever bw != 0, so this cannot borrow
+    r[0] -= bw & 38u;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h.v[k] = r[k];
+}
+
+FT_DEV void fe_neg(fe &h, const fe &f)
+{
+    fe z;
+    fe_0(z);
+    fe_sub(h, z, f);
+}
+
+// 512-bit t -> h < 2^256 with 2^256 = 38 (mod p)
+FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
+{
+    uint32_t r[8], r8;
+    r[0] = mad_lo_cc(t[8], 38u, t[0]);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r[k] = madc_lo_cc(t[8 + k], 38u, t[k]);
+    r8 = addc(0u, 0u);
+    r[1] = mad_hi_cc(t[8], 38u, r[1]);
+#pragma unroll
+    for (int k = 2; k < 8; ++k) r[k] = madc_hi_cc(t[7 + k], 38u, r[k]);
+    r8 = madc_hi(t[15], 38u, r8);
+    // value = r + r8 * 2^256 with r8 <= 38
+    r[0] = mad_lo_cc(r8, 38u, r[0]);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r[k] = addc_cc(r[k], 0u);
+    uint32_t c = addc(0u, 0u);
+    r[0] += 38u * c; // r < 1482 whenever c == 1
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h.v[k] = r[k];
+}
+
+// t = a * b (full 512-bit product), operand scanning in carry chains
+FT_DEV void mul_wide(uint32_t t[16], const fe &a, const fe &b)
+{
+#pragma unroll
+    for (int j = 0; j < 8; ++j) t[j] = mul_lo(a.v[0], b.v[j]);
+    t[1] = mad_hi_cc(a.v[0], b.v[0], t[1]);
+#pragma unroll
+    for (int j = 1; j < 7; ++j) t[j + 1] = madc_hi_cc(a.v[0], b.v[j], t[j + 1]);
+    t[8] = madc_hi(a.v[0], b.v[7], 0u);
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+        t[i] = mad_lo_cc(a.v[i], b.v[0], t[i]);
+#pragma unroll
+        for (int j = 1; j < 8; ++j) t[i + j] = madc_lo_cc(a.v[i], b.v[j], t[i + j]);
+        t[i + 8] = addc(0u, 0u);
+        t[i + 1] = mad_hi_cc(a.v[i], b.v[0], t[i + 1]);
+#pragma unroll
+        for (int j = 1; j < 7; ++j) t[i + j + 1] = madc_hi_cc(a.v[i], b.v[j], t[i + j + 1]);
+        t[i + 8] = madc_hi(a.v[i], b.v[7], t[i + 8]);
+    }
+}
+
+// t = a^2: 28 cross products doubled plus 8 squares
+FT_DEV void sqr_wide(uint32_t t[16], const fe &a)
+{
+    uint32_t c[16];
+    c[0] = 0u;
+    c[15] = 0u;
+#pragma unroll
+    for (int j = 1; j < 8; ++j) c[j] = mul_lo(a.v[0], a.v[j]);
+    c[2] = mad_hi_cc(a.v[0], a.v[1], c[2]);
+#pragma unroll
+    for (int j = 2; j < 7; ++j) c[j + 1] = madc_hi_cc(a.v[0], a.v[j], c[j + 1]);
+    c[8] = madc_hi(a.v[0], a.v[7], 0u);
+#pragma unroll
+    for (int i = 1; i < 6; ++i) {
+        c[2 * i + 1] = mad_lo_cc(a.v[i], a.v[i + 1], c[2 * i + 1]);
+#pragma unroll
+        for (int j = i + 2; j < 8; ++j) c[i + j] = madc_lo_cc(a.v[i], a.v[j], c[i + j]);
+        c[i + 8] = addc(0u, 0u);
+        c[2 * i + 2] = mad_hi_cc(a.v[i], a.v[i + 1], c[2 * i + 2]);
+#pragma unroll
+        for (int j = i + 2; j < 7; ++j) c[i + j + 1] = madc_hi_cc(a.v[i], a.v[j], c[i + j + 1]);
+        c[i + 8] = madc_hi(a.v[i], a.v[7], c[i + 8]);
+    }
+    // row 6: the single cross product a6 * a7 at position 13
+    c[13] = mad_lo_cc(a.v[6], a.v[7], c[13]);
+    c[14] = addc(0u, 0u);
+    c[14] = mad_hi_cc(a.v[6], a.v[7], c[14]);
+    // double the cross products
+    c[1] = add_cc(c[1], c[1]);
+#pragma unroll
+    for (int k = 2; k < 15; ++k) c[k] = addc_cc(c[k], c[k]);
+    c[15] = addc(0u, 0u);
+    // add the squares a_i^2 at positions 2i, 2i+1
+    t[0] = mul_lo(a.v[0], a.v[0]);
+    t[1] = mad_hi_cc(a.v[0], a.v[0], c[1]);
+#pragma unroll
+    for (int i = 1; i < 7; ++i) {
+        t[2 * i] = madc_lo_cc(a.v[i], a.v[i], c[2 * i]);
+        t[2 * i + 1] = madc_hi_cc(a.v[i], a.v[i], c[2 * i + 1]);
+    }
+    t[14] = madc_lo_cc(a.v[7], a.v[7], c[14]);
+    t[15] = madc_hi(a.v[7], a.v[7], c[15]);
+}
+
+FT_DEV void fe_mul(fe &h, const fe &a, const fe &b)
+{
+    uint32_t t[16];
+    mul_wide(t, a, b);
+    fe_fold512(h, t);
+}
+
+FT_DEV void fe_sq(fe &h, const fe &a)
+{
+    uint32_t t[16];
+    sqr_wide(t, a);
+    fe_fold512(h, t);
+}
+
+// 2 * a^2 (fe25519_sq2, sodium_fe.cu:1109)
+FT_DEV void fe_sq2(fe &h, const fe &a)
+{
+    fe s;
+    fe_sq(s, a);
+    fe_add(h, s, s);
+}
+
+// canonical representative in [0, p): fold bit 255 twice, then subtract p
+// once if needed (the reduction of fe25519_reduce, sodium_fe.cu:168-241)
+FT_DEV void fe_canon(fe &h, const fe &a)
+{
+    uint32_t v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = a.v[k];
+#pragma unroll
+    for (int round = 0; round < 2; ++round) {
+        uint32_t top = v[7] >> 31;
+        v[7] &= 0x7fffffffu;
+        v[0] = mad_lo_cc(top, 19u, v[0]);
+#pragma unroll
+        for (int k = 1; k < 7; ++k) v[k] = addc_cc(v[k], 0u);
+        v[7] = addc(v[7], 0u);
+    }
+    uint32_t u[8];
+    u[0] = add_cc(v[0], 19u);
+#pragma unroll
+    for (int k = 1; k < 7; ++k) u[k] = addc_cc(v[k], 0u);
+    u[7] = addc(v[7], 0u);
+    uint32_t m = 0u - (u[7] >> 31); // all ones iff v >= p
+    u[7] &= 0x7fffffffu;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h.v[k] = (v[k] & ~m) | (u[k] & m);
+}
+
+FT_DEV int fe_iszero(const fe &f)
+{
+    fe c;
+    fe_canon(c, f);
+    uint32_t o = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o |= c.v[k];
+    return o == 0;
+}
+
+FT_DEV uint32_t fe_isnegative(const fe &f)
+{
+    fe c;
+    fe_canon(c, f);
+    return c.v[0] & 1u;
+}
+
+// f = b ? g : f, for a mask b of all ones or all zeros
+FT_DEV void fe_cmov(fe &f, const fe &g, uint32_t mask)
+{
+#pragma unroll
+    for (int k = 0; k < 8; ++k) f.v[k] = (f.v[k] & ~mask) | (g.v[k] & mask);
+}
+
+FT_DEV void fe_copy(fe &h, const fe &f)
+{
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h.v[k] = f.v[k];
+}
+
+FT_DEV void fe_sqn(fe &h, const fe &f, int n)
+{
+    fe_sq(h, f);
+#pragma unroll 1
+    for (int i = 1; i < n; ++i) fe_sq(h, h);
+}
+
+// z^(p-2), the addition chain of fe25519_invert (sodium_fe.cu:1352-1408)
+FT_DEV void fe_invert(fe &out, const fe &z)
+{
+    fe t0, t1, t2, t3;
+    fe_sq(t0, z);
+    fe_sqn(t1, t0, 2);
+    fe_mul(t1, z, t1);
+    fe_mul(t0, t0, t1);
+    fe_sq(t2, t0);
+    fe_mul(t1, t1, t2);
+    fe_sqn(t2, t1, 5);
+    fe_mul(t1, t2, t1);
+    fe_sqn(t2, t1, 10);
+    fe_mul(t2, t2, t1);
+    fe_sqn(t3, t2, 20);
+    fe_mul(t2, t3, t2);
+    fe_sqn(t2, t2, 10);
+    fe_mul(t1, t2, t1);
+    fe_sqn(t2, t1, 50);
+    fe_mul(t2, t2, t1);
+    fe_sqn(t3, t2, 100);
+    fe_mul(t2, t3, t2);
+    fe_sqn(t2, t2, 50);
+    fe_mul(t1, t2, t1);
+    fe_sqn(t1, t1, 5);
+    fe_mul(out, t1, t0);
+}
+
+// z^((p-5)/8), the chain of fe25519_pow22523 (sodium_fe.cu:1410-1463)
+FT_DEV void fe_pow22523(fe &out, const fe &z)
+{
+    fe t0, t1, t2;
+    fe_sq(t0, z);
+    fe_sqn(t1, t0, 2);
+    fe_mul(t1, z, t1);
+    fe_mul(t0, t0, t1);
+    fe_sq(t0, t0);
+    fe_mul(t0, t1, t0);
+    fe_sqn(t1, t0, 5);
+    fe_mul(t0, t1, t0);
+    fe_sqn(t1, t0, 10);
+    fe_mul(t1, t1, t0);
+    fe_sqn(t2, t1, 20);
+    fe_mul(t1, t2, t1);
+    fe_sqn(t1, t1, 10);
+    fe_mul(t0, t1, t0);
+    fe_sqn(t1, t0, 50);
+    fe_mul(t1, t1, t0);
+    fe_sqn(t2, t1, 100);
+    fe_mul(t1, t2, t1);
+    fe_sqn(t1, t1, 50);
+    fe_mul(t0, t1, t0);
+    fe_sqn(t0, t0, 2);
+    fe_mul(out, t0, z);
+}
+
+// 32 little-endian bytes as 8 words, top bit ignored (fe25519_frombytes)
+FT_DEV void fe_from_words(fe &h, const uint32_t w[8])
+{
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h.v[k] = w[k];
+    h.v[7] &= 0x7fffffffu;
+}

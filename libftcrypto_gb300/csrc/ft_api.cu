@@ -1,0 +1,901 @@
+// ft_api.cu — the C ABI of include/ftcrypto.h and include/ftcrypto_gb300.h.
+//
+// Host logic for every entry point: argument checks with the reference's
+// error codes, stream-ordered device allocation from a private memory pool,
+// host<->device staging, and kernel launches (k_elem.cu, k_smul.cu,
+// k_reduce.cu).  All work is queued on one library stream; calls that return
+// host data synchronise that stream.  CUDA failures become FT_ERR_* codes;
+// nothing here exits the process.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "internal.h"
+#include "../../include/ftcrypto.h"
+#include "../../include/ftcrypto_gb300.h"
+
+using ft::View;
+
+namespace {
+
+struct Ctx {
+    bool inited = false;
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
+    void *scratch = nullptr;
+    size_t scratch_cap = 0;
+    long long *d_status = nullptr; // one device word for "last bad index"
+    ft_error last_void = FT_ERR_NO_ERROR;
+    uint8_t pk_bytes[32];
+    uint32_t *pk_table = nullptr; // comb table of the cached public key
+    bool pk_valid = false;
+};
+
+Ctx g;
+std::mutex g_init_mu;
+
+ft_error map_err(cudaError_t e)
+{
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? FT_ERR_OUT_OF_MEMORY : FT_ERR_INTERNAL_LIBRARY_ERROR;
+}
+
+#define CK(x)                                           \
+    do {                                                \
+        cudaError_t _e = (x);                           \
+        if (_e != cudaSuccess) return map_err(_e);      \
+    } while (0)
+
+#define ENSURE_INIT()                                   \
+    do {                                                \
+        if (!g.inited) {                                \
+            ft_error _ie = ft_crypto_init();            \
+            if (_ie) return _ie;                        \
+        }                                               \
+    } while (0)
+
+cudaError_t dev_alloc(void **p, size_t bytes)
+{
+    *p = nullptr;
+    if (bytes == 0) return cudaSuccess;
+    return cudaMallocFromPoolAsync(p, bytes, g.pool, g.stream);
+}
+
+void dev_free(void *p)
+{
+    if (p) cudaFreeAsync(p, g.stream);
+}
+
+// scratch of at least `bytes`, valid until the next scratch() call; stream
+// ordering makes reuse across calls safe
+cudaError_t scratch(void **p, size_t bytes)
+{
+    if (bytes > g.scratch_cap) {
+        dev_free(g.scratch);
+        g.scratch = nullptr;
+        g.scratch_cap = 0;
+        size_t cap = std::max(bytes, (size_t)1 << 20);
+        cudaError_t e = dev_alloc(&g.scratch, cap);
+        if (e != cudaSuccess) return e;
+        g.scratch_cap = cap;
+    }
+    *p = g.scratch;
+    return cudaSuccess;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+bool host_is_pinned(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// copy from caller memory: the caller may reuse `src` when this returns
+cudaError_t h2d(void *dst, const void *src, size_t bytes)
+{
+    if (bytes == 0) return cudaSuccess;
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g.stream);
+    if (e != cudaSuccess) return e;
+    // a pageable source is staged before cudaMemcpyAsync returns; a pinned
+    // one is read by DMA later, so wait for it
+    if (host_is_pinned(src)) e = cudaStreamSynchronize(g.stream);
+    return e;
+}
+
+cudaError_t d2h(void *dst, const void *src, size_t bytes)
+{
+    if (bytes) {
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g.stream);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaStreamSynchronize(g.stream);
+}
+
+ft_error arr_new(ft_ge25519_array *out, size_t n)
+{
+    auto *a = (ft_ge25519_array_s *)std::malloc(sizeof(ft_ge25519_array_s));
+    if (!a) return FT_ERR_OUT_OF_MEMORY;
+    a->n = n;
+    a->cap = n;
+    a->planes = nullptr;
+    cudaError_t e = dev_alloc((void **)&a->planes, n * FT_PLANES_BYTES_PER_POINT);
+    if (e != cudaSuccess) {
+        std::free(a);
+        return map_err(e);
+    }
+    *out = a;
+    return FT_ERR_NO_ERROR;
+}
+
+// replace the storage of a with a fresh buffer of `cap` points holding the
+// first `keep` points of the old one
+ft_error arr_realloc(ft_ge25519_array a, size_t cap, size_t keep)
+{
+    uint4 *np = nullptr;
+    CK(dev_alloc((void **)&np, cap * FT_PLANES_BYTES_PER_POINT));
+    cudaError_t e = ft::copy_points(View{np, cap}, ft::view_of(a), std::min(keep, cap), g.stream);
+    if (e != cudaSuccess) {
+        dev_free(np);
+        return map_err(e);
+    }
+    dev_free(a->planes);
+    a->planes = np;
+    a->cap = cap;
+    return FT_ERR_NO_ERROR;
+}
+
+template <class F>
+ft_error with_new_array(ft_ge25519_array *out, size_t n, F fill)
+{
+    ft_ge25519_array a;
+    ft_error err = arr_new(&a, n);
+    if (err) return err;
+    err = fill(a);
+    if (err) {
+        ft_array_free(a);
+        return err;
+    }
+    *out = a;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error check_idxs(const size_t *idxs, size_t n, size_t bound)
+{
+    for (size_t i = 0; i < n; ++i)
+        if (idxs[i] >= bound) return FT_ERR_OUT_OF_BOUNDS;
+    return FT_ERR_NO_ERROR;
+}
+
+// keep only the listed indices (ascending) of a
+ft_error compact(ft_ge25519_array a, const std::vector<uint64_t> &keep)
+{
+    size_t m = keep.size();
+    if (m == a->n) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(m * 8)));
+    CK(h2d(s, keep.data(), m * 8));
+    uint4 *np = nullptr;
+    CK(dev_alloc((void **)&np, m * FT_PLANES_BYTES_PER_POINT));
+    cudaError_t e = ft::gather(View{np, m}, ft::view_of(a), (const uint64_t *)s, m, g.stream);
+    if (e != cudaSuccess) {
+        dev_free(np);
+        return map_err(e);
+    }
+    dev_free(a->planes);
+    a->planes = np;
+    a->cap = m;
+    a->n = m;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error status_reset()
+{
+    CK(cudaMemsetAsync(g.d_status, 0xff, sizeof(long long), g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error status_read(int64_t *res)
+{
+    long long v = -1;
+    CK(d2h(&v, g.d_status, sizeof v));
+    *res = (int64_t)v;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ensure_pk_table(const uint8_t *pk)
+{
+    if (g.pk_valid && std::memcmp(g.pk_bytes, pk, 32) == 0) return FT_ERR_NO_ERROR;
+    g.pk_valid = false;
+    if (!g.pk_table) CK(dev_alloc((void **)&g.pk_table, 32 * 8 * 24 * sizeof(uint32_t)));
+    ft_ge25519_array q;
+    int64_t bad = -1;
+    ft_error err = ft_array_from_bytes_folded(&bad, &q, pk, 32);
+    if (err) return err;
+    if (bad >= 0) {
+        ft_array_free(q);
+        return FT_ERR_INVALID_POINT;
+    }
+    cudaError_t e = ft::build_comb_table(g.pk_table, ft::view_of(q), g.stream);
+    ft_array_free(q);
+    CK(e);
+    std::memcpy(g.pk_bytes, pk, 32);
+    g.pk_valid = true;
+    return FT_ERR_NO_ERROR;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *ft_error_str(ft_error err)
+{
+    // the reference's strings, ftcrypto.cu:34-57
+    static const char *errors[] = {"no error",
+                                   "out of memory",
+                                   "parameter sizes did not mmatch",
+                                   "bad size parameter",
+                                   "index out of bounds",
+                                   "invalid ed25519 point",
+                                   "failed to initialise libsodium",
+                                   "insufficient space in destination",
+                                   "ciphertext corrupted",
+                                   "internal library error",
+                                   "device or driver does not support a required feature"};
+    static_assert(sizeof(errors) / sizeof(errors[0]) == FT_ERR_MAX_ERR + 1, "error strings");
+    if (err < 0 || err > FT_ERR_MAX_ERR) return "bad error value";
+    return errors[err];
+}
+
+ft_error ft_crypto_init(void)
+{
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (g.inited) return FT_ERR_NO_ERROR;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return FT_ERR_INSUFFICIENT_DEVICE_OR_DRIVER;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return FT_ERR_INSUFFICIENT_DEVICE_OR_DRIVER;
+    }
+    // kernels are built for sm_103a only
+    if (prop.major != 10 || prop.minor != 3) return FT_ERR_INSUFFICIENT_DEVICE_OR_DRIVER;
+    CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    cudaMemPoolProps pp;
+    std::memset(&pp, 0, sizeof pp);
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.handleTypes = cudaMemHandleTypeNone;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = dev;
+    CK(cudaMemPoolCreate(&g.pool, &pp));
+    uint64_t thr = UINT64_MAX;
+    CK(cudaMemPoolSetAttribute(g.pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    g.device = dev;
+    CK(cudaMallocFromPoolAsync((void **)&g.d_status, 256, g.pool, g.stream));
+    CK(cudaStreamSynchronize(g.stream));
+    g.inited = true;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_crypto_device_memory(size_t *free_mem, size_t *total_mem)
+{
+    ENSURE_INIT();
+    CK(cudaMemGetInfo(free_mem, total_mem));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_init_scalar(ft_ge25519_array *array, size_t n, const uint8_t *scalar)
+{
+    ENSURE_INIT();
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        if (n == 0) return FT_ERR_NO_ERROR;
+        if (!scalar) {
+            CK(ft::set_zero(ft::view_of(a), n, g.stream));
+            return FT_ERR_NO_ERROR;
+        }
+        void *s;
+        CK(scratch(&s, 256));
+        CK(h2d(s, scalar, 32));
+        CK(ft::smul_base(ft::view_of(a), 1, (const uint8_t *)s, 0, g.stream));
+        CK(ft::broadcast(ft::view_of(a, 1), n - 1, ft::view_of(a), g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ft_array_init_point(ft_ge25519_array *array, size_t n, const_ft_ge25519_array src, size_t idx)
+{
+    ENSURE_INIT();
+    if (n > 0 && idx >= src->n) return FT_ERR_OUT_OF_BOUNDS;
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        CK(ft::broadcast(ft::view_of(a), n, ft::view_of(src, idx), g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ft_array_get_subset(ft_ge25519_array *array, const size_t *idxs, size_t n, const_ft_ge25519_array src)
+{
+    ENSURE_INIT();
+    ft_error err = check_idxs(idxs, n, src->n);
+    if (err) return err;
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        if (n == 0) return FT_ERR_NO_ERROR;
+        void *s;
+        CK(scratch(&s, align256(n * 8)));
+        CK(h2d(s, idxs, n * 8));
+        CK(ft::gather(ft::view_of(a), ft::view_of(src), (const uint64_t *)s, n, g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ft_array_get_range(ft_ge25519_array *array, size_t start, size_t stop, size_t step,
+                            const_ft_ge25519_array src)
+{
+    ENSURE_INIT();
+    size_t n = 0;
+    if (stop > start) {
+        if (step == 0) return FT_ERR_BAD_SIZE;
+        n = (stop - start) / step;
+    }
+    if (n > src->n) return FT_ERR_SIZE_MISMATCH;
+    if (n > 0 && start + (n - 1) * step >= src->n) return FT_ERR_OUT_OF_BOUNDS;
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        CK(ft::gather_range(ft::view_of(a), ft::view_of(src), start, step, n, g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ft_array_assign_to_subset(ft_ge25519_array array, const size_t *idxs, size_t n, const_ft_ge25519_array src)
+{
+    ENSURE_INIT();
+    if (n != src->n) return FT_ERR_SIZE_MISMATCH;
+    ft_error err = check_idxs(idxs, n, array->n);
+    if (err) return err;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 8)));
+    CK(h2d(s, idxs, n * 8));
+    CK(ft::scatter(ft::view_of(array), ft::view_of(src), (const uint64_t *)s, n, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_assign_zero_to_subset(ft_ge25519_array array, const size_t *idxs, size_t n)
+{
+    ENSURE_INIT();
+    ft_error err = check_idxs(idxs, n, array->n);
+    if (err) return err;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 8)));
+    CK(h2d(s, idxs, n * 8));
+    CK(ft::scatter_zero(ft::view_of(array), (const uint64_t *)s, n, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_assign_to_range(ft_ge25519_array array, size_t start, size_t stop, size_t step,
+                                  const_ft_ge25519_array src)
+{
+    ENSURE_INIT();
+    if (stop <= start) return FT_ERR_NO_ERROR;
+    if (step == 0) return FT_ERR_BAD_SIZE;
+    if ((stop - start) / step > src->n) return FT_ERR_SIZE_MISMATCH;
+    // the reference writes src[i] to start + i*step for every i < length(src)
+    // with start + i*step < stop (ftcrypto.cu:468-479)
+    size_t count = std::min(src->n, (stop - start + step - 1) / step);
+    if (count == 0) return FT_ERR_NO_ERROR;
+    if (start + (count - 1) * step >= array->n) return FT_ERR_OUT_OF_BOUNDS;
+    CK(ft::scatter_range(ft::view_of(array), ft::view_of(src), start, step, count, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_delete_subset(ft_ge25519_array array, const size_t *idxs, size_t n)
+{
+    ENSURE_INIT();
+    std::vector<size_t> del(idxs, idxs + n);
+    std::sort(del.begin(), del.end());
+    del.erase(std::unique(del.begin(), del.end()), del.end());
+    std::vector<uint64_t> keep;
+    keep.reserve(array->n);
+    size_t d = 0;
+    for (size_t i = 0; i < array->n; ++i) {
+        while (d < del.size() && del[d] < i) ++d;
+        if (d < del.size() && del[d] == i) continue;
+        keep.push_back(i);
+    }
+    return compact(array, keep);
+}
+
+ft_error ft_array_delete_range(ft_ge25519_array array, size_t start, size_t stop, size_t step)
+{
+    ENSURE_INIT();
+    if (stop > start && step == 0) return FT_ERR_BAD_SIZE;
+    std::vector<uint64_t> keep;
+    keep.reserve(array->n);
+    for (size_t i = 0; i < array->n; ++i) {
+        if (i >= start && i < stop && (i - start) % step == 0) continue;
+        keep.push_back(i);
+    }
+    return compact(array, keep);
+}
+
+ft_error ft_array_to_bytes_folded(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array array)
+{
+    ENSURE_INIT();
+    size_t n = array->n;
+    if (n_bytes / FT_FOLDED_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 32)));
+    CK(ft::encode((uint8_t *)s, ft::view_of(array), n, g.stream));
+    CK(d2h(mem, s, n * 32));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_to_bytes_affine(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array array)
+{
+    ENSURE_INIT();
+    size_t n = array->n;
+    if (n_bytes / FT_AFFINE_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 64)));
+    CK(ft::to_affine((uint8_t *)s, ft::view_of(array), n, g.stream));
+    CK(d2h(mem, s, n * 64));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_to_bytes(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array array)
+{
+    ENSURE_INIT();
+    size_t n = array->n;
+    if (n_bytes / FT_EXTENDED_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 160)));
+    CK(ft::to_ref160((uint8_t *)s, ft::view_of(array), n, g.stream));
+    CK(d2h(mem, s, n * 160));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_from_bytes_folded(int64_t *res, ft_ge25519_array *array, const uint8_t *mem, size_t n_bytes)
+{
+    ENSURE_INIT();
+    if (n_bytes % FT_FOLDED_POINT_BYTES) return FT_ERR_BAD_SIZE;
+    size_t n = n_bytes / FT_FOLDED_POINT_BYTES;
+    int64_t bad = -1;
+    ft_error err = with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        if (n == 0) return FT_ERR_NO_ERROR;
+        void *s;
+        CK(scratch(&s, align256(n_bytes)));
+        CK(h2d(s, mem, n_bytes));
+        ft_error e2 = status_reset();
+        if (e2) return e2;
+        CK(ft::decode(ft::view_of(a), (const uint8_t *)s, n, g.d_status, g.stream));
+        return status_read(&bad);
+    });
+    if (err) return err;
+    *res = bad;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_from_bytes_affine(ft_ge25519_array *array, const uint8_t *mem, size_t n_bytes)
+{
+    ENSURE_INIT();
+    if (n_bytes % FT_AFFINE_POINT_BYTES) return FT_ERR_BAD_SIZE;
+    size_t n = n_bytes / FT_AFFINE_POINT_BYTES;
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        if (n == 0) return FT_ERR_NO_ERROR;
+        void *s;
+        CK(scratch(&s, align256(n_bytes)));
+        CK(h2d(s, mem, n_bytes));
+        CK(ft::from_affine(ft::view_of(a), (const uint8_t *)s, n, g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ft_array_from_bytes(ft_ge25519_array *array, const uint8_t *mem, size_t n_bytes)
+{
+    ENSURE_INIT();
+    if (n_bytes % FT_EXTENDED_POINT_BYTES) return FT_ERR_BAD_SIZE;
+    size_t n = n_bytes / FT_EXTENDED_POINT_BYTES;
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        if (n == 0) return FT_ERR_NO_ERROR;
+        void *s;
+        CK(scratch(&s, align256(n_bytes)));
+        CK(h2d(s, mem, n_bytes));
+        CK(ft::from_ref160(ft::view_of(a), (const uint8_t *)s, n, g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ft_array_validate(int64_t *res, const_ft_ge25519_array array)
+{
+    ENSURE_INIT();
+    ft_error err = status_reset();
+    if (err) return err;
+    CK(ft::validate(ft::view_of(array), array->n, g.d_status, g.stream));
+    return status_read(res);
+}
+
+ft_error ft_array_from_scalars(ft_ge25519_array *array, const uint8_t *scalars, size_t n)
+{
+    ENSURE_INIT();
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        if (n == 0) return FT_ERR_NO_ERROR;
+        void *s;
+        CK(scratch(&s, align256(n * 32)));
+        CK(h2d(s, scalars, n * 32));
+        CK(ft::smul_base(ft::view_of(a), n, (const uint8_t *)s, 1, g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ft_array_from_small_scalars(ft_ge25519_array *array, const uint64_t *small, size_t n)
+{
+    ENSURE_INIT();
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        if (n == 0) return FT_ERR_NO_ERROR;
+        void *s;
+        CK(scratch(&s, align256(n * 8)));
+        CK(h2d(s, small, n * 8));
+        CK(ft::smul_base_small(ft::view_of(a), n, (const uint64_t *)s, g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+void ft_array_free(ft_ge25519_array array)
+{
+    if (!array) return;
+    if (g.inited) dev_free(array->planes);
+    std::free(array);
+}
+
+size_t ft_array_get_length(const_ft_ge25519_array array) { return array->n; }
+
+// ftcrypto.cu:291-336
+ft_error ft_array_set_length(ft_ge25519_array array, size_t newlen)
+{
+    ENSURE_INIT();
+    size_t len = array->n;
+    if (newlen <= len / 2) {
+        ft_error err = arr_realloc(array, newlen, newlen);
+        if (err) return err;
+        array->n = newlen;
+    } else if (newlen <= len) {
+        array->n = newlen;
+    } else if (newlen <= array->cap) {
+        CK(ft::set_zero(ft::view_of(array, len), newlen - len, g.stream));
+        array->n = newlen;
+    } else {
+        ft_error err = arr_realloc(array, newlen, len);
+        if (err) return err;
+        CK(ft::set_zero(ft::view_of(array, len), newlen - len, g.stream));
+        array->n = newlen;
+    }
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_mux(ft_ge25519_array iftrue, const int64_t *cond, const_ft_ge25519_array iffalse)
+{
+    ENSURE_INIT();
+    if (iftrue->n != iffalse->n) return FT_ERR_SIZE_MISMATCH;
+    size_t n = iftrue->n;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 8)));
+    CK(h2d(s, cond, n * 8));
+    CK(ft::mux(ft::view_of(iftrue), (const int64_t *)s, ft::view_of(iffalse), n, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_contains(int64_t *res, const_ft_ge25519_array array1, const_ft_ge25519_array array2)
+{
+    ENSURE_INIT();
+    size_t n1 = array1->n, n2 = array2->n;
+    std::vector<uint8_t> e1(n1 * 32), e2(n2 * 32);
+    ft_error err;
+    if ((err = ft_array_to_bytes_folded(e1.data(), e1.size(), array1))) return err;
+    if ((err = ft_array_to_bytes_folded(e2.data(), e2.size(), array2))) return err;
+    std::vector<const uint8_t *> keys(n2);
+    for (size_t j = 0; j < n2; ++j) keys[j] = e2.data() + 32 * j;
+    auto lt = [](const uint8_t *a, const uint8_t *b) { return std::memcmp(a, b, 32) < 0; };
+    std::sort(keys.begin(), keys.end(), lt);
+    for (size_t i = 0; i < n1; ++i) res[i] = std::binary_search(keys.begin(), keys.end(), e1.data() + 32 * i, lt);
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_add(ft_ge25519_array res, const_ft_ge25519_array summand)
+{
+    ENSURE_INIT();
+    if (summand->n != res->n) return FT_ERR_SIZE_MISMATCH;
+    CK(ft::add(ft::view_of(res), ft::view_of(summand), res->n, 0, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_reduce_isum(ft_ge25519_array res, const size_t *idxs, size_t n, const_ft_ge25519_array src)
+{
+    ENSURE_INIT();
+    if (n != src->n) return FT_ERR_SIZE_MISMATCH;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    size_t nk = res->n;
+    if (n >= (size_t)INT32_MAX || nk >= (size_t)INT32_MAX) return FT_ERR_BAD_SIZE;
+    ft_error err = check_idxs(idxs, n, nk);
+    if (err) return err;
+    size_t b_keys = align256(n * 8), b_off = align256((nk + 1) * 4), b_perm = align256(n * 4);
+    size_t b_sort = align256(ft::isum_scratch_bytes(n, nk));
+    void *s;
+    CK(scratch(&s, b_keys + b_off + b_perm + b_sort));
+    uint8_t *base = (uint8_t *)s;
+    uint64_t *keys = (uint64_t *)base;
+    int32_t *off = (int32_t *)(base + b_keys);
+    int32_t *perm = (int32_t *)(base + b_keys + b_off);
+    void *sort_tmp = base + b_keys + b_off + b_perm;
+    CK(h2d(keys, idxs, n * 8));
+    if ((err = status_reset())) return err;
+    CK(ft::keys_to_csr(off, perm, keys, n, nk, g.d_status, sort_tmp, g.stream));
+    CK(ft::segsum(ft::view_of(res), off, nk, ft::view_of(src), n, perm, 1, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_sub(ft_ge25519_array res, const_ft_ge25519_array summand)
+{
+    ENSURE_INIT();
+    if (summand->n != res->n) return FT_ERR_SIZE_MISMATCH;
+    CK(ft::add(ft::view_of(res), ft::view_of(summand), res->n, 1, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+static ft_error scale_impl(ft_ge25519_array array, const uint8_t *scalar)
+{
+    ENSURE_INIT();
+    if (array->n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, 256));
+    CK(h2d(s, scalar, 32));
+    CK(ft::smul_var(ft::view_of(array), array->n, (const uint8_t *)s, 0, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+void ft_scale(ft_ge25519_array array, const uint8_t *scalar) { g.last_void = scale_impl(array, scalar); }
+
+static ft_error neg_impl(ft_ge25519_array array)
+{
+    ENSURE_INIT();
+    CK(ft::neg(ft::view_of(array), array->n, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+void ft_neg(ft_ge25519_array array) { g.last_void = neg_impl(array); }
+
+ft_error ft_mul(ft_ge25519_array array, const uint8_t *scalars, size_t n)
+{
+    ENSURE_INIT();
+    if (n != array->n) return FT_ERR_SIZE_MISMATCH;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 32)));
+    CK(h2d(s, scalars, n * 32));
+    CK(ft::smul_var(ft::view_of(array), n, (const uint8_t *)s, 1, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+static ft_error index_impl(int64_t *res, const_ft_ge25519_array array)
+{
+    ENSURE_INIT();
+    size_t n = array->n;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 8)));
+    CK(ft::index_nonzero((int64_t *)s, ft::view_of(array), n, g.stream));
+    CK(d2h(res, s, n * 8));
+    return FT_ERR_NO_ERROR;
+}
+
+void ft_index(int64_t *res, const_ft_ge25519_array array) { g.last_void = index_impl(res, array); }
+
+static ft_error equal_impl(int64_t *res, const_ft_ge25519_array a, const_ft_ge25519_array b, int invert)
+{
+    ENSURE_INIT();
+    if (a->n != b->n) return FT_ERR_SIZE_MISMATCH;
+    size_t n = a->n;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 8)));
+    CK(ft::equal((int64_t *)s, ft::view_of(a), ft::view_of(b), n, invert, g.stream));
+    CK(d2h(res, s, n * 8));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_equal(int64_t *res, const_ft_ge25519_array a, const_ft_ge25519_array b) { return equal_impl(res, a, b, 0); }
+ft_error ft_not_equal(int64_t *res, const_ft_ge25519_array a, const_ft_ge25519_array b) { return equal_impl(res, a, b, 1); }
+
+static ft_error scan_impl(ft_ge25519_array array, int exclusive)
+{
+    ENSURE_INIT();
+    size_t n = array->n;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, ft::scan_scratch_bytes(n)));
+    CK(ft::scan(ft::view_of(array), n, exclusive, s, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ft_array_prescan(ft_ge25519_array array) { return scan_impl(array, 1); }
+ft_error ft_array_scan(ft_ge25519_array array) { return scan_impl(array, 0); }
+
+ft_error ft_array_reduce(ft_ge25519_array array)
+{
+    ENSURE_INIT();
+    size_t n = array->n;
+    if (n == 1) return FT_ERR_NO_ERROR;
+    uint4 *np = nullptr;
+    CK(dev_alloc((void **)&np, FT_PLANES_BYTES_PER_POINT));
+    void *s;
+    cudaError_t e = scratch(&s, ft::reduce_scratch_bytes(n));
+    if (e == cudaSuccess) e = ft::reduce(View{np, 1}, ft::view_of(array), n, s, g.stream);
+    if (e != cudaSuccess) {
+        dev_free(np);
+        return map_err(e);
+    }
+    dev_free(array->planes);
+    array->planes = np;
+    array->n = 1;
+    array->cap = 1;
+    return FT_ERR_NO_ERROR;
+}
+
+// ---------------------------------------------------------------- extensions
+
+ft_error ftx_last_error(void) { return g.last_void; }
+
+void *ftx_stream(void)
+{
+    if (!g.inited && ft_crypto_init()) return nullptr;
+    return (void *)g.stream;
+}
+
+ft_error ftx_synchronize(void)
+{
+    ENSURE_INIT();
+    CK(cudaStreamSynchronize(g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_array_device_view(const_ft_ge25519_array array, void **planes, size_t *stride)
+{
+    *planes = (void *)array->planes;
+    *stride = array->cap;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_array_to_packed(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array array)
+{
+    ENSURE_INIT();
+    size_t n = array->n;
+    if (n_bytes / 128 < n) return FT_ERR_INSUFFICIENT_SPACE;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 128)));
+    CK(ft::to_packed((uint8_t *)s, ft::view_of(array), n, g.stream));
+    CK(d2h(mem, s, n * 128));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_array_from_packed(ft_ge25519_array *array, const uint8_t *mem, size_t n_bytes)
+{
+    ENSURE_INIT();
+    if (n_bytes % 128) return FT_ERR_BAD_SIZE;
+    size_t n = n_bytes / 128;
+    return with_new_array(array, n, [&](ft_ge25519_array a) -> ft_error {
+        if (n == 0) return FT_ERR_NO_ERROR;
+        void *s;
+        CK(scratch(&s, align256(n_bytes)));
+        CK(h2d(s, mem, n_bytes));
+        CK(ft::from_packed(ft::view_of(a), (const uint8_t *)s, n, g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ftx_mul_device(ft_ge25519_array array, const uint8_t *d_scalars, size_t n)
+{
+    ENSURE_INIT();
+    if (n != array->n) return FT_ERR_SIZE_MISMATCH;
+    CK(ft::smul_var(ft::view_of(array), n, d_scalars, 1, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+static int m_digits(unsigned bits) { return (int)((bits + 3) / 4) + 1; }
+
+ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint64_t *d_m,
+                            const uint8_t *d_r, size_t n, unsigned bits)
+{
+    ENSURE_INIT();
+    if (bits < 1 || bits > 64) return FT_ERR_BAD_SIZE;
+    if (c1->n != n || c2->n != n) return FT_ERR_SIZE_MISMATCH;
+    ft_error err = ensure_pk_table(pk);
+    if (err) return err;
+    CK(ft::encrypt(ft::view_of(c1), ft::view_of(c2), n, d_r, d_m, m_digits(bits), g.pk_table, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *pk, const uint64_t *m,
+                     const uint8_t *r, size_t n, unsigned bits)
+{
+    ENSURE_INIT();
+    if (bits < 1 || bits > 64) return FT_ERR_BAD_SIZE;
+    if (bits < 64)
+        for (size_t i = 0; i < n; ++i)
+            if (m[i] >> bits) return FT_ERR_BAD_SIZE;
+    ft_error err = ensure_pk_table(pk);
+    if (err) return err;
+    ft_ge25519_array a, b;
+    if ((err = arr_new(&a, n))) return err;
+    if ((err = arr_new(&b, n))) {
+        ft_array_free(a);
+        return err;
+    }
+    void *s;
+    size_t br = align256(n * 32);
+    cudaError_t e = scratch(&s, br + align256(n * 8));
+    if (e == cudaSuccess) e = h2d(s, r, n * 32);
+    if (e == cudaSuccess) e = h2d((uint8_t *)s + br, m, n * 8);
+    if (e == cudaSuccess)
+        e = ft::encrypt(ft::view_of(a), ft::view_of(b), n, (const uint8_t *)s, (const uint64_t *)((uint8_t *)s + br),
+                        m_digits(bits), g.pk_table, g.stream);
+    if (e != cudaSuccess) {
+        ft_array_free(a);
+        ft_array_free(b);
+        return map_err(e);
+    }
+    *c1 = a;
+    *c2 = b;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_segmented_sum_csr_device(ft_ge25519_array out, const int32_t *d_off, size_t nseg,
+                                      const_ft_ge25519_array src)
+{
+    ENSURE_INIT();
+    if (out->n != nseg) return FT_ERR_SIZE_MISMATCH;
+    if (src->n >= (size_t)INT32_MAX || nseg >= (size_t)INT32_MAX) return FT_ERR_BAD_SIZE;
+    CK(ft::segsum(ft::view_of(out), d_off, nseg, ft::view_of(src), src->n, nullptr, 0, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_segmented_sum_csr(ft_ge25519_array *out, const int32_t *off, size_t nseg, const_ft_ge25519_array src)
+{
+    ENSURE_INIT();
+    if (src->n >= (size_t)INT32_MAX || nseg >= (size_t)INT32_MAX) return FT_ERR_BAD_SIZE;
+    if (off[0] != 0 || (size_t)off[nseg] != src->n) return FT_ERR_BAD_SIZE;
+    for (size_t s = 0; s < nseg; ++s)
+        if (off[s + 1] < off[s]) return FT_ERR_BAD_SIZE;
+    return with_new_array(out, nseg, [&](ft_ge25519_array a) -> ft_error {
+        if (nseg == 0) return FT_ERR_NO_ERROR;
+        void *s;
+        CK(scratch(&s, align256((nseg + 1) * 4)));
+        CK(h2d(s, off, (nseg + 1) * 4));
+        CK(ft::segsum(ft::view_of(a), (const int32_t *)s, nseg, ft::view_of(src), src->n, nullptr, 0, g.stream));
+        return FT_ERR_NO_ERROR;
+    });
+}
+
+ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_array src)
+{
+    ENSURE_INIT();
+    if (out_idx >= out->n) return FT_ERR_OUT_OF_BOUNDS;
+    void *s;
+    CK(scratch(&s, ft::reduce_scratch_bytes(src->n)));
+    CK(ft::reduce(ft::view_of(out, out_idx), ft::view_of(src), src->n, s, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+} // extern "C"

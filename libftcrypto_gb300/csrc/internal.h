@@ -1,0 +1,83 @@
+// internal.h — declarations shared by the host API (ft_api.cu) and the
+// kernel translation units (k_*.cu).  Not installed; the public interface is
+// include/ftcrypto.h and include/ftcrypto_gb300.h.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifndef FT_PLANES
+#define FT_PLANES 8
+#endif
+#define FT_PLANES_BYTES_PER_POINT ((size_t)FT_PLANES * 16)
+
+// An array handle: device-resident structure-of-arrays planes (points.cuh).
+struct ft_ge25519_array_s {
+    uint4 *planes; // FT_PLANES planes of `cap` uint4 each (NULL when cap == 0)
+    size_t n;      // number of points
+    size_t cap;    // plane stride = number of points allocated
+};
+
+namespace ft {
+
+// A view of n points starting at element `off` of an array.
+struct View {
+    uint4 *p;
+    size_t s; // plane stride
+};
+
+inline View view_of(const ft_ge25519_array_s *a, size_t off = 0) { return View{a->planes + off, a->cap}; }
+
+// ---- element-wise (k_elem.cu)
+cudaError_t set_zero(View v, size_t n, cudaStream_t st);
+cudaError_t broadcast(View dst, size_t n, View src, cudaStream_t st);
+cudaError_t add(View res, View src, size_t n, int sub, cudaStream_t st);
+cudaError_t neg(View v, size_t n, cudaStream_t st);
+cudaError_t index_nonzero(int64_t *d_out, View v, size_t n, cudaStream_t st);
+cudaError_t equal(int64_t *d_out, View a, View b, size_t n, int invert, cudaStream_t st);
+cudaError_t mux(View t, const int64_t *d_cond, View f, size_t n, cudaStream_t st);
+cudaError_t gather(View dst, View src, const uint64_t *d_idx, size_t n, cudaStream_t st);
+cudaError_t scatter(View dst, View src, const uint64_t *d_idx, size_t n, cudaStream_t st);
+cudaError_t scatter_zero(View dst, const uint64_t *d_idx, size_t n, cudaStream_t st);
+cudaError_t gather_range(View dst, View src, size_t start, size_t step, size_t n, cudaStream_t st);
+cudaError_t scatter_range(View dst, View src, size_t start, size_t step, size_t n, cudaStream_t st);
+cudaError_t copy_points(View dst, View src, size_t n, cudaStream_t st);
+cudaError_t encode(uint8_t *d_out32, View v, size_t n, cudaStream_t st);
+cudaError_t decode(View v, const uint8_t *d_in32, size_t n, long long *d_bad, cudaStream_t st);
+cudaError_t to_affine(uint8_t *d_out64, View v, size_t n, cudaStream_t st);
+cudaError_t from_affine(View v, const uint8_t *d_in64, size_t n, cudaStream_t st);
+cudaError_t to_ref160(uint8_t *d_out160, View v, size_t n, cudaStream_t st);
+cudaError_t from_ref160(View v, const uint8_t *d_in160, size_t n, cudaStream_t st);
+cudaError_t to_packed(uint8_t *d_out128, View v, size_t n, cudaStream_t st);
+cudaError_t from_packed(View v, const uint8_t *d_in128, size_t n, cudaStream_t st);
+cudaError_t validate(View v, size_t n, long long *d_bad, cudaStream_t st);
+
+// ---- scalar multiplication (k_smul.cu)
+// per-element (sc_step = 1) or broadcast (sc_step = 0) 32-byte scalars
+cudaError_t smul_var(View v, size_t n, const uint8_t *d_scalars, int sc_step, cudaStream_t st);
+cudaError_t smul_base(View v, size_t n, const uint8_t *d_scalars, int sc_step, cudaStream_t st);
+cudaError_t smul_base_small(View v, size_t n, const uint64_t *d_small, cudaStream_t st);
+// affine comb table of Q (32 x 8 x 24 words) from the point at element 0 of q
+cudaError_t build_comb_table(uint32_t *d_table, View q, cudaStream_t st);
+// c1 = r*B, c2 = m*B + r*PK; pk_table from build_comb_table
+cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *d_r, const uint64_t *d_m,
+                    int m_digits, const uint32_t *d_pk_table, cudaStream_t st);
+int smul_var_block();
+
+// ---- reductions (k_reduce.cu)
+size_t reduce_scratch_bytes(size_t n);
+cudaError_t reduce(View out, View src, size_t n, void *d_scratch, cudaStream_t st);
+size_t scan_scratch_bytes(size_t n);
+cudaError_t scan(View v, size_t n, int exclusive, void *d_scratch, cudaStream_t st);
+// out[s] (+)= sum of src[perm ? perm[e] : e] for e in [off[s], off[s+1])
+cudaError_t segsum(View out, const int32_t *d_off, size_t nseg, View src, size_t nsrc,
+                   const int32_t *d_perm, int accumulate, cudaStream_t st);
+// counting sort of keys < nkeys: d_off (nkeys + 1) and d_perm (n); *d_bad set to
+// the largest out-of-range position, or left at -1
+size_t isum_scratch_bytes(size_t n, size_t nkeys);
+cudaError_t keys_to_csr(int32_t *d_off, int32_t *d_perm, const uint64_t *d_keys, size_t n,
+                        size_t nkeys, long long *d_bad, void *d_scratch, cudaStream_t st);
+
+int sm_count();
+
+} // namespace ft

@@ -1,0 +1,138 @@
+// smul.cuh — per-thread scalar multiplication cores.
+//
+//   smul_build_table / smul_ladder : constant-time variable-base a*P in the
+//       reference's signed radix-16 window (ge25519_scalarmult,
+//       sodium_ge.cu:650-731): table (k+1)*P for k < 8 built in the same
+//       order, 63 x {select, add, 4 doublings} + final add.  The table lives
+//       wherever the caller's accessor puts it (shared memory in the kernels).
+//   comb_accumulate : the fixed-base comb of ge25519_scalarmult_base
+//       (sodium_ge.cu:743-792) over a 32 x 8 affine table
+//       table[i][j] = (j+1) * 256^i * Q, selected in constant time.
+#pragma once
+#include "ge.cuh"
+
+// Tab: put(k, const ge_cached&), get(k, ge_cached&) for k in [0, 8)
+template <class Tab>
+FT_DEV void smul_build_table(Tab &tab, const ge_p3 &p)
+{
+    ge_cached c;
+    ge_p1p1 t;
+    ge_p3 p2, p3, p4, q;
+    ge_p3_to_cached(c, p);
+    tab.put(0, c); // 1P
+    ge_p3_dbl(t, p);
+    ge_p1p1_to_p3(p2, t);
+    ge_p3_to_cached(c, p2);
+    tab.put(1, c); // 2P = 2*P
+    ge_add(t, p, c);
+    ge_p1p1_to_p3(p3, t);
+    ge_p3_to_cached(c, p3);
+    tab.put(2, c); // 3P = P + 2P
+    ge_p3_dbl(t, p2);
+    ge_p1p1_to_p3(p4, t);
+    ge_p3_to_cached(c, p4);
+    tab.put(3, c); // 4P = 2*2P
+    ge_add(t, p, c);
+    ge_p1p1_to_p3(q, t);
+    ge_p3_to_cached(c, q);
+    tab.put(4, c); // 5P = P + 4P
+    ge_p3_dbl(t, p3);
+    ge_p1p1_to_p3(q, t);
+    ge_p3_to_cached(c, q);
+    tab.put(5, c); // 6P = 2*3P
+    ge_add(t, p, c);
+    ge_p1p1_to_p3(q, t);
+    ge_p3_to_cached(c, q);
+    tab.put(6, c); // 7P = P + 6P
+    ge_p3_dbl(t, p4);
+    ge_p1p1_to_p3(q, t);
+    ge_p3_to_cached(c, q);
+    tab.put(7, c); // 8P = 2*4P
+}
+
+// h = a * P where tab holds (k+1)*P.  a is 8 little-endian words.
+template <class Tab>
+FT_DEV void smul_ladder(ge_p3 &h, const uint32_t a[8], const Tab &tab)
+{
+    uint32_t b[8];
+    recode_bias(b, a);
+    ge_p3_0(h);
+    ge_p1p1 r;
+    ge_p2 s;
+    ge_cached t;
+    auto get = [&](int k, ge_cached &e) { tab.get(k, e); };
+    int d = pop_top_nibble(b); // digit 63 carries no bias
+#pragma unroll 1
+    for (int i = 63; i > 0; --i) {
+        select_cached(t, d, get);
+        ge_add(r, h, t);
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            ge_p1p1_to_p2(s, r);
+            ge_p2_dbl(r, s);
+        }
+        ge_p1p1_to_p3(h, r);
+        d = pop_top_nibble(b) - 8;
+    }
+    select_cached(t, d, get);
+    ge_add(r, h, t);
+    ge_p1p1_to_p3(h, r);
+}
+
+FT_DEV void shr8_256(uint32_t c[8])
+{
+#pragma unroll
+    for (int k = 0; k < 7; ++k) c[k] = (c[k] >> 8) | (c[k + 1] << 24);
+    c[7] >>= 8;
+}
+
+// h += sum over rows r < nrows of digit(2r + parity) * table[r], where the
+// digits come from the biased recoding b (see recode_bias).
+// Get: get(row, k, ge_precomp&) returns (k+1) * 256^row * Q.
+template <class Get>
+FT_DEV void comb_accumulate(ge_p3 &h, const uint32_t b[8], int parity, int nrows, Get get)
+{
+    uint32_t c[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) c[k] = b[k];
+    ge_p1p1 r;
+    ge_precomp t;
+#pragma unroll 1
+    for (int row = 0; row < nrows; ++row) {
+        int i = 2 * row + parity;
+        int d = (int)((c[0] >> (4 * parity)) & 15u) - (i == 63 ? 0 : 8);
+        shr8_256(c);
+        select_precomp(t, d, [&](int k, ge_precomp &e) { get(row, k, e); });
+        ge_madd(r, h, t);
+        ge_p1p1_to_p3(h, r);
+    }
+}
+
+// h = 16 * h through the doubling sequence of sodium_ge.cu:778-785
+FT_DEV void ge_mul16(ge_p3 &h)
+{
+    ge_p1p1 r;
+    ge_p2 s;
+    ge_p3_dbl(r, h);
+    ge_p1p1_to_p2(s, r);
+    ge_p2_dbl(r, s);
+    ge_p1p1_to_p2(s, r);
+    ge_p2_dbl(r, s);
+    ge_p1p1_to_p2(s, r);
+    ge_p2_dbl(r, s);
+    ge_p1p1_to_p3(h, r);
+}
+
+// h = a * Q by the comb (ge25519_scalarmult_base, sodium_ge.cu:743-792),
+// restricted to the first `ndigits` radix-16 digits (64 for a full scalar;
+// fewer when a is publicly known to be small).
+template <class Get>
+FT_DEV void comb_mul(ge_p3 &h, const uint32_t a[8], int ndigits, Get get)
+{
+    uint32_t b[8];
+    recode_bias(b, a);
+    ge_p3_0(h);
+    comb_accumulate(h, b, 1, ndigits / 2, get);
+    ge_mul16(h);
+    comb_accumulate(h, b, 0, (ndigits + 1) / 2, get);
+}

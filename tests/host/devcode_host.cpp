@@ -1,0 +1,91 @@
+// devcode_host.cpp — host build of the library's per-thread device arithmetic
+// (fe.cuh, ge.cuh, smul.cuh) over the C stand-ins of ptx_emul.h, exported for
+// tests/test_devcode_host.py to compare with the oracle.  TEST HARNESS ONLY.
+#include <string.h>
+#include "../../libftcrypto_gb300/csrc/smul.cuh"
+#define FT_TABLE_QUAL static const
+#define FT_WANT_BASE_COMB
+#include "../../libftcrypto_gb300/csrc/base_table.inc"
+
+static void ld(ge_p3 &p, const uint8_t *s) { memcpy(p.X.v, s, 32); memcpy(p.Y.v, s + 32, 32); memcpy(p.Z.v, s + 64, 32); memcpy(p.T.v, s + 96, 32); }
+static void st(uint8_t *s, const ge_p3 &p) { memcpy(s, p.X.v, 32); memcpy(s + 32, p.Y.v, 32); memcpy(s + 64, p.Z.v, 32); memcpy(s + 96, p.T.v, 32); }
+
+struct ArrTab {
+    ge_cached e[8];
+    void put(int k, const ge_cached &c) { e[k] = c; }
+    void get(int k, ge_cached &c) const { c = e[k]; }
+};
+
+static void base_entry(int row, int k, ge_precomp &e)
+{
+    const uint32_t *w = FT_BASE_COMB_INIT + (row * 8 + k) * 24;
+    memcpy(e.yplusx.v, w, 32);
+    memcpy(e.yminusx.v, w + 8, 32);
+    memcpy(e.xy2d.v, w + 16, 32);
+}
+
+extern "C" {
+
+void hc_fe_mul(uint32_t *h, const uint32_t *a, const uint32_t *b)
+{
+    fe x, y, z;
+    memcpy(x.v, a, 32); memcpy(y.v, b, 32);
+    fe_mul(z, x, y);
+    memcpy(h, z.v, 32);
+}
+void hc_fe_sq(uint32_t *h, const uint32_t *a) { fe x, z; memcpy(x.v, a, 32); fe_sq(z, x); memcpy(h, z.v, 32); }
+void hc_fe_add(uint32_t *h, const uint32_t *a, const uint32_t *b) { fe x, y, z; memcpy(x.v, a, 32); memcpy(y.v, b, 32); fe_add(z, x, y); memcpy(h, z.v, 32); }
+void hc_fe_sub(uint32_t *h, const uint32_t *a, const uint32_t *b) { fe x, y, z; memcpy(x.v, a, 32); memcpy(y.v, b, 32); fe_sub(z, x, y); memcpy(h, z.v, 32); }
+void hc_fe_canon(uint32_t *h, const uint32_t *a) { fe x, z; memcpy(x.v, a, 32); fe_canon(z, x); memcpy(h, z.v, 32); }
+void hc_fe_invert(uint32_t *h, const uint32_t *a) { fe x, z; memcpy(x.v, a, 32); fe_invert(z, x); memcpy(h, z.v, 32); }
+
+void hc_add(uint8_t *res, const uint8_t *b, size_t n)
+{
+    for (size_t i = 0; i < n; ++i) { ge_p3 p, q; ld(p, res + 128 * i); ld(q, b + 128 * i); ge_addto(p, q); st(res + 128 * i, p); }
+}
+void hc_sub(uint8_t *res, const uint8_t *b, size_t n)
+{
+    for (size_t i = 0; i < n; ++i) { ge_p3 p, q; ld(p, res + 128 * i); ld(q, b + 128 * i); ge_subfrom(p, q); st(res + 128 * i, p); }
+}
+void hc_mul(uint8_t *pts, const uint8_t *scalars, size_t n)
+{
+    for (size_t i = 0; i < n; ++i) {
+        ge_p3 p, h; ArrTab tab; uint32_t a[8];
+        ld(p, pts + 128 * i); memcpy(a, scalars + 32 * i, 32);
+        smul_build_table(tab, p);
+        smul_ladder(h, a, tab);
+        st(pts + 128 * i, h);
+    }
+}
+void hc_comb(uint8_t *pts, const uint8_t *scalars, size_t n, int ndigits)
+{
+    for (size_t i = 0; i < n; ++i) {
+        ge_p3 h; uint32_t a[8];
+        memcpy(a, scalars + 32 * i, 32);
+        comb_mul(h, a, ndigits, base_entry);
+        st(pts + 128 * i, h);
+    }
+}
+void hc_encode(uint8_t *out, const uint8_t *pts, size_t n)
+{
+    for (size_t i = 0; i < n; ++i) {
+        ge_p3 p; fe zi; uint32_t w[8];
+        ld(p, pts + 128 * i);
+        fe_invert(zi, p.Z);
+        ge_encode_with_zinv(w, p, zi);
+        memcpy(out + 32 * i, w, 32);
+    }
+}
+long long hc_decode(uint8_t *pts, const uint8_t *in, size_t n)
+{
+    long long bad = -1;
+    for (size_t i = 0; i < n; ++i) {
+        ge_p3 p; uint32_t w[8];
+        memcpy(w, in + 32 * i, 32);
+        if (ge_frombytes(p, w)) bad = (long long)i;
+        st(pts + 128 * i, p);
+    }
+    return bad;
+}
+
+} // extern "C"

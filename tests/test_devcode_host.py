@@ -1,0 +1,100 @@
+"""The library's per-thread device arithmetic (csrc/fe.cuh, ge.cuh, smul.cuh),
+compiled for the host over C stand-ins of its PTX carry primitives
+(tests/host/ptx_emul.h), against Python integers and the oracle.  Catches
+arithmetic errors without a GPU; the GPU tests check the real kernels."""
+import ctypes
+import os
+import random
+import subprocess
+
+import numpy as np
+import pytest
+
+from libftcrypto_gb300 import synth
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+P = 2**255 - 19
+
+
+@pytest.fixture(scope="module")
+def hc(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("hc") / "devcode_host.so")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared",
+                           '-DFT_HOST_EMULATION="../../tests/host/ptx_emul.h"', "-o", so,
+                           os.path.join(HERE, "host", "devcode_host.cpp")])
+    return ctypes.CDLL(so)
+
+
+def w(x):
+    return (ctypes.c_uint32 * 8)(*[(x >> (32 * i)) & 0xFFFFFFFF for i in range(8)])
+
+
+def v(a):
+    return sum(int(a[i]) << (32 * i) for i in range(8))
+
+
+def ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def test_field_ops(hc):
+    rnd = random.Random(5)
+    edge = [0, 1, 2, 19, 38, P - 1, P, P + 1, 2 * P - 1, 2 * P, 2**255 - 1, 2**255, 2**256 - 1,
+            2**256 - 38, 2**256 - 39, 2**256 - 20]
+    vals = edge + [rnd.getrandbits(256) for _ in range(1500)]
+    out = (ctypes.c_uint32 * 8)()
+    for i, a in enumerate(vals):
+        b = vals[(7 * i + 3) % len(vals)]
+        for fn, want in ((hc.hc_fe_mul, a * b), (hc.hc_fe_add, a + b), (hc.hc_fe_sub, a - b)):
+            fn(out, w(a), w(b))
+            assert v(out) < 2**256 and v(out) % P == want % P
+        hc.hc_fe_sq(out, w(a))
+        assert v(out) < 2**256 and v(out) % P == a * a % P
+        hc.hc_fe_canon(out, w(a))
+        assert v(out) == a % P
+    for a in vals[:100]:
+        hc.hc_fe_invert(out, w(a))
+        assert v(out) % P == pow(a, P - 2, P)
+
+
+def test_group_and_smul(hc, orc):
+    g = synth.rng(3)
+    n = 48
+    sc = synth.scalars_mod_L(g, n)
+    for i, x in enumerate([0, 1, synth.L - 1, 2**256 - 1, 2**255 + 12345]):
+        sc[i] = synth.int_to_scalar(x)
+    p1 = orc.from_scalars(sc)
+    p2 = orc.from_scalars(np.ascontiguousarray(sc[::-1]))
+    a = p1.copy()
+    hc.hc_add(ptr(a), ptr(p2), n)
+    assert (orc.encode(a) == orc.encode(orc.add(p1, p2))).all()
+    s = p1.copy()
+    hc.hc_sub(ptr(s), ptr(p2), n)
+    assert (orc.encode(s) == orc.encode(orc.sub(p1, p2))).all()
+    m = p1.copy()
+    hc.hc_mul(ptr(m), ptr(sc), n)
+    om = orc.mul(p1, sc)
+    assert (m == om).all()  # same formula sequence: identical coordinates
+    c = np.zeros_like(p1)
+    hc.hc_comb(ptr(c), ptr(sc), n, 64)
+    assert (orc.encode(c) == orc.encode(p1)).all()
+    e = np.zeros((n, 32), np.uint8)
+    hc.hc_encode(ptr(e), ptr(om), n)
+    assert (e == orc.encode(om)).all()
+
+
+def test_decode_and_small_comb(hc, orc):
+    g = synth.rng(4)
+    good = orc.encode(orc.from_scalars(synth.scalars_mod_L(g, 20)))
+    inp = np.concatenate([good, g.integers(0, 256, (100, 32), dtype=np.uint8)])
+    d = np.zeros((inp.shape[0], 128), np.uint8)
+    hc.hc_decode.restype = ctypes.c_longlong
+    bad = hc.hc_decode(ptr(d), ptr(inp), inp.shape[0])
+    od, obad = orc.decode(inp)
+    assert bad == obad
+    assert (orc.encode(d) == orc.encode(od)).all()
+    m = np.array([0, 1, 255, 2**32, 2**64 - 1] + list(range(7, 22)), dtype=np.uint64)
+    small = orc.small_to_scalars(m)
+    c = np.zeros((len(m), 128), np.uint8)
+    hc.hc_comb(ptr(c), ptr(small), len(m), 17)
+    assert (orc.encode(c) == orc.encode(orc.from_scalars(small))).all()
