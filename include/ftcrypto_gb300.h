@@ -68,6 +68,21 @@ ft_error ftx_segmented_sum_csr_device(ft_ge25519_array out, const int32_t *d_off
 /* out[out_idx] = sum of src, leaving src unchanged. */
 ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_array src);
 
+/* Prefix scan (exclusive if `exclusive` is non-zero, else inclusive) of n
+ * points that the caller keeps in its own device memory, in this library's
+ * layout (8 planes of 16-byte words, plane stride `stride` >= n, see
+ * ftx_array_device_view), queued on the caller's CUDA stream.  No
+ * counterpart in the reference: it exists for callers that cannot allocate
+ * device memory (their memory is held by another allocator, or they must not
+ * trigger cudaMalloc's synchronisation).  It allocates nothing; the scan's
+ * scratch is a fixed array of about 17 MB that the library keeps on every
+ * GPU that loads it.  n <= FT_NOALLOC_SCAN_MAX_POINTS (FT_ERR_BAD_SIZE
+ * otherwise).  All calls share that array: calls that overlap on the GPU
+ * race and must be serialised.  The first call on a device looks up the
+ * array's address; make it before any stream capture. */
+#define FT_NOALLOC_SCAN_MAX_POINTS 1048576
+ft_error ftx_scan_noalloc(void *d_planes, size_t stride, size_t n, int exclusive, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,6 +73,7 @@ SIGNATURES = {
     "ftx_segmented_sum_csr": (I, [PP, P, S, P]),
     "ftx_segmented_sum_csr_device": (I, [P, P, S, P]),
     "ftx_reduce_into": (I, [P, S, P]),
+    "ftx_scan_noalloc": (I, [P, S, S, I, P]),
 }
 
 REFERENCE_SYMBOLS = [k for k in SIGNATURES if k.startswith("ft_")]

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libftcrypto.so")
 BENCH_LIB = os.path.join(HERE, "libftbench.so")  # bench.py's integer-pipe peak probe
-SOURCES = ["ft_api.cu", "k_elem.cu", "k_smul.cu", "k_reduce.cu"]
+SOURCES = ["ft_api.cu", "k_elem.cu", "k_smul.cu", "k_reduce.cu", "k_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--extended-lambda"]
 

@@ -1,0 +1,90 @@
+// k_noalloc.cu — ftx_scan_noalloc: the prefix scan of ft_array_scan /
+// ft_array_prescan without any device allocation.
+//
+// Who needs it: callers that cannot call cudaMalloc — for example a host
+// framework whose caching allocator already holds the GPU's memory and hands
+// out only its own buffers, or a latency-bound caller that must not trigger
+// the implicit synchronisation cudaMalloc / cudaFree can cause.  They pass
+// the points (their own device buffer, in this library's plane layout) and a
+// stream; the scan's scratch (per-thread and per-chunk partial sums) comes
+// from a fixed array compiled into this library instead of the allocator.
+//
+// Limits and sharing:
+//  * at most FT_NOALLOC_SCAN_MAX_POINTS points per call (FT_ERR_BAD_SIZE
+//    beyond it); the array is FT_NOALLOC_SCAN_SCRATCH_BYTES (about 17 MB) and
+//    is resident on every GPU that loads the library until the process exits;
+//  * every call uses the same array and leaves its partial sums there; each
+//    launch writes all scratch it later reads, so nothing must start at zero;
+//  * calls whose work overlaps on the GPU (different streams, or different
+//    host threads) race on the array and give wrong results: serialise them.
+//  * the first call on each device looks up the array's device address
+//    (cudaGetSymbolAddress) with that device current; make that first call
+//    before any stream capture.
+#include <mutex>
+
+#include "internal.h"
+#include "../../include/ftcrypto.h"
+#include "../../include/ftcrypto_gb300.h"
+
+// scratch layout of ft::scan at the maximum size: per level, one point per
+// thread of each 1024-point chunk plus one per chunk (see k_reduce.cu)
+static constexpr size_t noalloc_scan_points(size_t n)
+{
+    size_t pts = 0;
+    while (n > 1) {
+        size_t nch = (n + 1023) / 1024;
+        pts += nch * 128 + nch;
+        n = nch;
+    }
+    return pts;
+}
+
+static constexpr size_t FT_NOALLOC_SCAN_SCRATCH_BYTES =
+    ((noalloc_scan_points(FT_NOALLOC_SCAN_MAX_POINTS) * 128 + 256 + 255) / 256) * 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[FT_NOALLOC_SCAN_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void *g_addr[kMaxDevices];
+
+// device address of the scratch array on the current device (once per device)
+cudaError_t scratch_address(void **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
+        if (e != cudaSuccess) return e;
+        g_addr[dev] = p;
+    }
+    *out = g_addr[dev];
+    return cudaSuccess;
+}
+
+} // namespace
+
+extern "C" ft_error ftx_scan_noalloc(void *d_planes, size_t stride, size_t n, int exclusive, void *stream)
+{
+    if (n > FT_NOALLOC_SCAN_MAX_POINTS) return FT_ERR_BAD_SIZE;
+    if (n > stride) return FT_ERR_SIZE_MISMATCH;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    static_assert(noalloc_scan_points(FT_NOALLOC_SCAN_MAX_POINTS) * 128 + 256 <= FT_NOALLOC_SCAN_SCRATCH_BYTES,
+                  "scratch covers the largest scan");
+    if (ft::scan_scratch_bytes(n) > FT_NOALLOC_SCAN_SCRATCH_BYTES) return FT_ERR_INTERNAL_LIBRARY_ERROR;
+    void *scratch = nullptr;
+    cudaError_t e = scratch_address(&scratch);
+    if (e == cudaSuccess)
+        e = ft::scan(ft::View{(uint4 *)d_planes, stride}, n, exclusive ? 1 : 0, scratch, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return FT_ERR_INTERNAL_LIBRARY_ERROR;
+    }
+    return FT_ERR_NO_ERROR;
+}
