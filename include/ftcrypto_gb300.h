@@ -68,6 +68,13 @@ ft_error ftx_segmented_sum_csr_device(ft_ge25519_array out, const int32_t *d_off
 /* out[out_idx] = sum of src, leaving src unchanged. */
 ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_array src);
 
+/* Launch-shape knobs, set by the autotuner (libftcrypto_gb300/autotune.py)
+ * or by hand.  ftx_tune returns FT_ERR_BAD_SIZE for an unsupported value;
+ * ftx_tune_get returns the current value (-1 for an unknown knob). */
+#define FTX_TUNE_LADDER_BLOCK 1 /* variable-base ladder block size: 128, 192 or 224 */
+ft_error ftx_tune(int knob, int value);
+int ftx_tune_get(int knob);
+
 /* Prefix scan (exclusive if `exclusive` is non-zero, else inclusive) of n
  * points that the caller keeps in its own device memory, in this library's
  * layout (8 planes of 16-byte words, plane stride `stride` >= n, see

@@ -73,6 +73,8 @@ SIGNATURES = {
     "ftx_segmented_sum_csr": (I, [PP, P, S, P]),
     "ftx_segmented_sum_csr_device": (I, [P, P, S, P]),
     "ftx_reduce_into": (I, [P, S, P]),
+    "ftx_tune": (I, [I, I]),
+    "ftx_tune_get": (I, [I]),
     "ftx_scan_noalloc": (I, [P, S, S, I, P]),
 }
 

@@ -17,7 +17,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libftcrypto.so")
 BENCH_LIB = os.path.join(HERE, "libftbench.so")  # bench.py's integer-pipe peak probe
-SOURCES = ["ft_api.cu", "k_elem.cu", "k_smul.cu", "k_reduce.cu", "k_noalloc.cu"]
+# (source, object, extra defines): k_ladder.cu is compiled once per block size
+LADDER_BLOCKS = (128, 192, 224)
+SOURCES = [(s, s.replace(".cu", ".o"), []) for s in ("ft_api.cu", "k_elem.cu", "k_smul.cu", "k_reduce.cu",
+                                                     "k_noalloc.cu")]
+SOURCES += [("k_ladder.cu", f"k_ladder_{nt}.o", [f"-DFT_LADDER_NT={nt}"]) for nt in LADDER_BLOCKS]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--extended-lambda"]
 
@@ -49,12 +53,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     procs = []
-    for src in SOURCES:
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [cc] + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+    for src, objname, defs in SOURCES:
+        obj = os.path.join(BUILD, objname)
+        cmd = [cc] + FLAGS + defs + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
-        procs.append((src, obj, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+        procs.append((objname, obj, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     objs = []
     failed = []
     for src, obj, p in procs:
@@ -67,7 +71,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + ".tmp"
     subprocess.check_call([cc] + ARCH + ["-shared", "-o", tmp] + objs)
     os.replace(tmp, LIB)
-    subprocess.check_call([cc] + FLAGS + ["-shared", "-o", BENCH_LIB, os.path.join(CSRC, "bench_peak.cu")])
+    bench_src = os.path.join(CSRC, "bench_peak.cu")
+    if force or not os.path.exists(BENCH_LIB) or os.path.getmtime(BENCH_LIB) < os.path.getmtime(bench_src):
+        subprocess.check_call([cc] + FLAGS + ["-shared", "-o", BENCH_LIB, bench_src])
     return LIB
 
 

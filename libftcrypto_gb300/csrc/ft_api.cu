@@ -888,6 +888,22 @@ ft_error ftx_segmented_sum_csr(ft_ge25519_array *out, const int32_t *off, size_t
     });
 }
 
+ft_error ftx_tune(int knob, int value)
+{
+    switch (knob) {
+    case FTX_TUNE_LADDER_BLOCK: return ft::set_ladder_block(value) ? FT_ERR_BAD_SIZE : FT_ERR_NO_ERROR;
+    default: return FT_ERR_BAD_SIZE;
+    }
+}
+
+int ftx_tune_get(int knob)
+{
+    switch (knob) {
+    case FTX_TUNE_LADDER_BLOCK: return ft::ladder_block();
+    default: return -1;
+    }
+}
+
 ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_array src)
 {
     ENSURE_INIT();

@@ -62,7 +62,12 @@ cudaError_t build_comb_table(uint32_t *d_table, View q, cudaStream_t st);
 // c1 = r*B, c2 = m*B + r*PK; pk_table from build_comb_table
 cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *d_r, const uint64_t *d_m,
                     int m_digits, const uint32_t *d_pk_table, cudaStream_t st);
-int smul_var_block();
+// ladder instantiations (k_ladder.cu) and the run-time block-size knob
+cudaError_t ladder_launch_128(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
+cudaError_t ladder_launch_192(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
+cudaError_t ladder_launch_224(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
+int ladder_block();
+int set_ladder_block(int nt);
 
 // ---- reductions (k_reduce.cu)
 size_t reduce_scratch_bytes(size_t n);

@@ -1,11 +1,7 @@
 // k_smul.cu — scalar multiplication kernels.
 //
-//   k_smul_var   constant-time variable-base a_i * P_i (ft_mul / ft_scale;
-//                k_ft_mul and k_ft_scale, ftcrypto.cu:966-994).  Each thread
-//                keeps its 8-entry cached table (1 KB) in shared memory laid
-//                out [entry][16-byte word][thread] so every table access of a
-//                warp is 512 contiguous bytes (conflict-free); the table is
-//                scanned in full under masks for each digit.
+//   smul_var     dispatch of the constant-time variable-base ladder
+//                (ladder.cuh, one instantiation per block size in k_ladder.cu)
 //   k_comb_base  a_i * B by the fixed-base comb over the 24 KB table of
 //                (j+1)*256^i*B staged in shared memory (ft_array_from_scalars,
 //                ft_array_from_small_scalars, ft_array_init_scalar).  The
@@ -17,6 +13,7 @@
 #include "internal.h"
 #include "points.cuh"
 #include "smul.cuh"
+#include "ladder.cuh"
 
 #define FT_TABLE_QUAL static __device__ __align__(16) const
 #define FT_WANT_BASE_COMB
@@ -25,55 +22,6 @@
 namespace ft {
 
 #define COMB_U4 (32 * 8 * 6) // uint4 words in one comb table (24 KB)
-
-// per-thread cached table in shared memory
-template <int NT>
-struct SmemTab {
-    uint4 *b; // &smem[threadIdx.x]
-    FT_DEV void put(int k, const ge_cached &c) const
-    {
-        uint4 *q = b + (size_t)k * 8 * NT;
-        q[0 * NT] = u4_lo(c.YplusX);
-        q[1 * NT] = u4_hi(c.YplusX);
-        q[2 * NT] = u4_lo(c.YminusX);
-        q[3 * NT] = u4_hi(c.YminusX);
-        q[4 * NT] = u4_lo(c.Z);
-        q[5 * NT] = u4_hi(c.Z);
-        q[6 * NT] = u4_lo(c.T2d);
-        q[7 * NT] = u4_hi(c.T2d);
-    }
-    FT_DEV void get(int k, ge_cached &c) const
-    {
-        const uint4 *q = b + (size_t)k * 8 * NT;
-        fe_from_u4(c.YplusX, q[0 * NT], q[1 * NT]);
-        fe_from_u4(c.YminusX, q[2 * NT], q[3 * NT]);
-        fe_from_u4(c.Z, q[4 * NT], q[5 * NT]);
-        fe_from_u4(c.T2d, q[6 * NT], q[7 * NT]);
-    }
-};
-
-FT_DEV void load_scalar(uint32_t a[8], const uint4 *sc, size_t i)
-{
-    uint4 s0 = sc[2 * i], s1 = sc[2 * i + 1];
-    a[0] = s0.x; a[1] = s0.y; a[2] = s0.z; a[3] = s0.w;
-    a[4] = s1.x; a[5] = s1.y; a[6] = s1.z; a[7] = s1.w;
-}
-
-template <int NT>
-__global__ void __launch_bounds__(NT, 1) k_smul_var(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step)
-{
-    extern __shared__ uint4 smem[];
-    size_t i = (size_t)blockIdx.x * NT + threadIdx.x;
-    if (i >= n) return;
-    SmemTab<NT> tab{smem + threadIdx.x};
-    ge_p3 P, h;
-    ld_p3(P, p, s, i);
-    uint32_t a[8];
-    load_scalar(a, sc, i * (size_t)sc_step);
-    smul_build_table(tab, P);
-    smul_ladder(h, a, tab);
-    st_p3(p, s, i, h);
-}
 
 // comb table entry (row, k) of a table of COMB_U4 uint4 in shared memory
 FT_DEV void comb_get(const uint4 *t, int row, int k, ge_precomp &e)
@@ -90,16 +38,31 @@ FT_DEV void stage_table(uint4 *dst, const uint4 *src)
     __syncthreads();
 }
 
+// One comb row: h += digit * table[row] with the digit taken from the low
+// byte of c (nibble `parity`) and c shifted down by one byte.  The kernels
+// below run all of their rows through one loop so this body, the hot code,
+// exists once in the instruction stream (separate inlined passes made the
+// encrypt kernel stall on instruction fetch).
+FT_DEV void comb_row(ge_p3 &h, uint32_t c[8], int parity, int row, bool top, const uint4 *tab)
+{
+    int d = (int)((c[0] >> (4 * parity)) & 15u) - (top ? 0 : 8);
+    shr8_256(c);
+    ge_precomp t;
+    select_precomp(t, d, [&](int k, ge_precomp &e) { comb_get(tab, row, k, e); });
+    ge_p1p1 r;
+    ge_madd(r, h, t);
+    ge_p1p1_to_p3(h, r);
+}
+
 // mode 0: 32-byte scalars (sc_step 0 = one scalar for all); mode 1: uint64
 __global__ void __launch_bounds__(128) k_comb_base(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step,
                                                    const uint64_t *small)
 {
     __shared__ uint4 tb[COMB_U4];
     stage_table(tb, (const uint4 *)FT_BASE_COMB_INIT);
-    auto get = [&](int row, int k, ge_precomp &e) { comb_get(tb, row, k, e); };
     FT_GRID_LOOP(i, n)
     {
-        uint32_t a[8];
+        uint32_t a[8], b[8];
         int nd = 64;
         if (small) {
             uint64_t m = small[i];
@@ -111,8 +74,21 @@ __global__ void __launch_bounds__(128) k_comb_base(uint4 *p, size_t s, size_t n,
         } else {
             load_scalar(a, sc, i * (size_t)sc_step);
         }
+        recode_bias(b, a);
         ge_p3 h;
-        comb_mul(h, a, nd, get);
+        ge_p3_0(h);
+        // pass 0: odd digits, then 16*h; pass 1: even digits (sodium_ge.cu:772-791)
+#pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            const int parity = 1 - pass;
+            const int nrows = parity ? nd / 2 : (nd + 1) / 2;
+            uint32_t c[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) c[k] = b[k];
+#pragma unroll 1
+            for (int row = 0; row < nrows; ++row) comb_row(h, c, parity, row, 2 * row + parity == 63, tb);
+            if (pass == 0) ge_mul16(h);
+        }
         st_p3(p, s, i, h);
     }
 }
@@ -127,8 +103,6 @@ __global__ void __launch_bounds__(128) k_encrypt(uint4 *c1, size_t s1, uint4 *c2
         tp[j] = pktab[j];
     }
     __syncthreads();
-    auto getb = [&](int row, int k, ge_precomp &e) { comb_get(tb, row, k, e); };
-    auto getp = [&](int row, int k, ge_precomp &e) { comb_get(tp, row, k, e); };
     FT_GRID_LOOP(i, n)
     {
         uint32_t a[8], br[8], bm[8], mw[8];
@@ -141,19 +115,29 @@ __global__ void __launch_bounds__(128) k_encrypt(uint4 *c1, size_t s1, uint4 *c2
         for (int k = 2; k < 8; ++k) mw[k] = 0;
         recode_bias(bm, mw);
         ge_p3 h;
-        // c1 = r * B
         ge_p3_0(h);
-        comb_accumulate(h, br, 1, 32, getb);
-        ge_mul16(h);
-        comb_accumulate(h, br, 0, 32, getb);
-        st_p3(c1, s1, i, h);
-        // c2 = r * PK + m * B in one accumulator
-        ge_p3_0(h);
-        comb_accumulate(h, br, 1, 32, getp);
-        comb_accumulate(h, bm, 1, mdig / 2, getb);
-        ge_mul16(h);
-        comb_accumulate(h, br, 0, 32, getp);
-        comb_accumulate(h, bm, 0, (mdig + 1) / 2, getb);
+        // c1 = r*B: pass 0 odd digits of r, 16*h, pass 1 even digits.
+        // c2 = r*PK + m*B in one accumulator: pass 2 odd digits of r (PK
+        // table), pass 3 odd digits of m (B table), 16*h, pass 4 even
+        // digits of r (PK), pass 5 even digits of m (B).
+#pragma unroll 1
+        for (int pass = 0; pass < 6; ++pass) {
+            const bool use_m = pass == 3 || pass == 5;
+            const int parity = (pass == 0 || pass == 2 || pass == 3) ? 1 : 0;
+            const uint4 *tab = (pass == 2 || pass == 4) ? tp : tb;
+            const int nrows = use_m ? (parity ? mdig / 2 : (mdig + 1) / 2) : 32;
+            uint32_t c[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) c[k] = use_m ? bm[k] : br[k];
+#pragma unroll 1
+            for (int row = 0; row < nrows; ++row)
+                comb_row(h, c, parity, row, !use_m && 2 * row + parity == 63, tab);
+            if (pass == 0 || pass == 3) ge_mul16(h);
+            if (pass == 1) {
+                st_p3(c1, s1, i, h);
+                ge_p3_0(h);
+            }
+        }
         st_p3(c2, s2, i, h);
     }
 }
@@ -202,23 +186,26 @@ __global__ void __launch_bounds__(256) k_comb_table(uint4 *out, const uint4 *q, 
 
 // ------------------------------------------------------------ launchers
 
-static const int SMUL_NT = 128;
-static const size_t SMUL_SMEM = (size_t)SMUL_NT * 8 * 8 * sizeof(uint4);
+static int g_ladder_nt = 224;
 
-int smul_var_block() { return SMUL_NT; }
+int ladder_block() { return g_ladder_nt; }
+
+int set_ladder_block(int nt)
+{
+    if (nt != 128 && nt != 192 && nt != 224) return -1;
+    g_ladder_nt = nt;
+    return 0;
+}
 
 cudaError_t smul_var(View v, size_t n, const uint8_t *sc, int sc_step, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_smul_var<SMUL_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMUL_SMEM);
-        if (e != cudaSuccess) return e;
-        attr = true;
+    const uint4 *s4 = (const uint4 *)sc;
+    switch (g_ladder_nt) {
+    case 128: return ladder_launch_128(v.p, v.s, n, s4, sc_step, st);
+    case 192: return ladder_launch_192(v.p, v.s, n, s4, sc_step, st);
+    default: return ladder_launch_224(v.p, v.s, n, s4, sc_step, st);
     }
-    unsigned grid = (unsigned)((n + SMUL_NT - 1) / SMUL_NT);
-    k_smul_var<SMUL_NT><<<grid, SMUL_NT, SMUL_SMEM, st>>>(v.p, v.s, n, (const uint4 *)sc, sc_step);
-    return cudaGetLastError();
 }
 
 static unsigned comb_grid(size_t n)

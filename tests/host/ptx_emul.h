@@ -23,3 +23,4 @@ static inline uint32_t mad_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint64_t 
 static inline uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint64_t t = (((uint64_t)a * b) >> 32) + c + g_cf; g_cf = (uint32_t)(t >> 32); return (uint32_t)t; }
 static inline uint32_t madc_hi(uint32_t a, uint32_t b, uint32_t c) { return (uint32_t)(((uint64_t)a * b) >> 32) + c + g_cf; }
 static inline uint32_t mul_lo(uint32_t a, uint32_t b) { return a * b; }
+static inline uint32_t mul_hi(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
