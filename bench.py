@@ -507,6 +507,73 @@ def run_ours(args):
     return 0
 
 
+PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "reduce", "scan", "segsum", "isum", "encode", "decode")
+
+
+def run_profile(case: str) -> int:
+    """One small run of one kernel family, for ncu (profiles/*.md): inputs are
+    built, then the operation runs twice (the second launch is the one to
+    capture with `-s <setup launches + 1> -c 1` or `-k regex:<kernel>`)."""
+    import torch
+    import libftcrypto_gb300 as ft
+    from libftcrypto_gb300 import synth
+    ft.build()
+    ft.init()
+    g = synth.rng(SEED + 99)
+    n = 1 << 20
+    sc = synth.scalars_mod_L(g, n)
+    d_sc = torch.from_numpy(sc).cuda()
+    torch.cuda.synchronize()
+    base = ft.Array.from_scalars(sc[:4096])
+    if case == "ladder":
+        a = ft.Array.init_point(n, base, 1)
+        op = lambda: a.mul_device(d_sc.data_ptr(), n)  # noqa: E731
+    elif case == "encrypt":
+        pk = base.get_subset([0]).to_bytes_folded()[0]
+        m = torch.from_numpy(to_i64(synth.plaintexts(g, n, 255))).cuda()
+        torch.cuda.synchronize()
+        c1, c2 = ft.Array.init_scalar(n), ft.Array.init_scalar(n)
+        op = lambda: ft.encrypt_device(c1, c2, pk, m.data_ptr(), d_sc.data_ptr(), n, 8)  # noqa: E731
+    elif case == "comb":
+        op = lambda: ft.Array.from_scalars(sc)  # noqa: E731
+    elif case in ("add", "reduce", "scan", "segsum", "isum"):
+        big = 1 << 24 if case in ("reduce", "segsum") else 1 << 22
+        a = ft.Array.init_point(big, base, 3)
+        a.add(ft.Array.init_point(big, base, 5))
+        if case == "add":
+            b = ft.Array.init_point(big, base, 7)
+            op = lambda: a.add(b)  # noqa: E731
+        elif case == "reduce":
+            out = ft.Array.init_scalar(1)
+            op = lambda: a.reduce_into(out, 0)  # noqa: E731
+        elif case == "scan":
+            op = lambda: a.scan()  # noqa: E731
+        elif case == "segsum":
+            off = synth.csr_offsets(g, big, big // 16)
+            d_off = torch.from_numpy(off).cuda()
+            torch.cuda.synchronize()
+            out = ft.Array.init_scalar(big // 16)
+            op = lambda: ft.segmented_sum_csr_device(out, d_off.data_ptr(), big // 16, a)  # noqa: E731
+        else:
+            keys = g.integers(0, big // 16, big).astype(np.uint64)
+            res = ft.Array.init_scalar(big // 16)
+            op = lambda: res.reduce_isum(keys, a)  # noqa: E731
+    elif case == "encode":
+        a = ft.Array.init_point(n, base, 1)
+        a.mul_device(d_sc.data_ptr(), n)
+        op = lambda: a.to_bytes_folded()  # noqa: E731
+    elif case == "decode":
+        enc = ft.Array.from_scalars(sc).to_bytes_folded()
+        op = lambda: ft.Array.from_bytes_folded(enc)  # noqa: E731
+    else:
+        raise SystemExit(f"unknown case {case}")
+    op()
+    op()
+    ft.synchronize()
+    print(json.dumps({"profile_case": case, "ok": True}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -514,7 +581,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--profile", choices=PROFILE_CASES, help="run one kernel family once, for ncu")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args.profile)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -632,8 +632,9 @@ ft_error ft_reduce_isum(ft_ge25519_array res, const size_t *idxs, size_t n, cons
     if (err) return err;
     size_t b_keys = align256(n * 8), b_off = align256((nk + 1) * 4), b_perm = align256(n * 4);
     size_t b_sort = align256(ft::isum_scratch_bytes(n, nk));
+    size_t b_seg = align256(ft::segsum_scratch_bytes(n));
     void *s;
-    CK(scratch(&s, b_keys + b_off + b_perm + b_sort));
+    CK(scratch(&s, b_keys + b_off + b_perm + b_sort + b_seg));
     uint8_t *base = (uint8_t *)s;
     uint64_t *keys = (uint64_t *)base;
     int32_t *off = (int32_t *)(base + b_keys);
@@ -642,7 +643,8 @@ ft_error ft_reduce_isum(ft_ge25519_array res, const size_t *idxs, size_t n, cons
     CK(h2d(keys, idxs, n * 8));
     if ((err = status_reset())) return err;
     CK(ft::keys_to_csr(off, perm, keys, n, nk, g.d_status, sort_tmp, g.stream));
-    CK(ft::segsum(ft::view_of(res), off, nk, ft::view_of(src), n, perm, 1, g.stream));
+    void *seg_tmp = base + b_keys + b_off + b_perm + b_sort;
+    CK(ft::segsum(ft::view_of(res), off, nk, ft::view_of(src), n, perm, 1, seg_tmp, g.stream));
     return FT_ERR_NO_ERROR;
 }
 
@@ -867,7 +869,9 @@ ft_error ftx_segmented_sum_csr_device(ft_ge25519_array out, const int32_t *d_off
     ENSURE_INIT();
     if (out->n != nseg) return FT_ERR_SIZE_MISMATCH;
     if (src->n >= (size_t)INT32_MAX || nseg >= (size_t)INT32_MAX) return FT_ERR_BAD_SIZE;
-    CK(ft::segsum(ft::view_of(out), d_off, nseg, ft::view_of(src), src->n, nullptr, 0, g.stream));
+    void *s;
+    CK(scratch(&s, ft::segsum_scratch_bytes(src->n)));
+    CK(ft::segsum(ft::view_of(out), d_off, nseg, ft::view_of(src), src->n, nullptr, 0, s, g.stream));
     return FT_ERR_NO_ERROR;
 }
 
@@ -881,9 +885,11 @@ ft_error ftx_segmented_sum_csr(ft_ge25519_array *out, const int32_t *off, size_t
     return with_new_array(out, nseg, [&](ft_ge25519_array a) -> ft_error {
         if (nseg == 0) return FT_ERR_NO_ERROR;
         void *s;
-        CK(scratch(&s, align256((nseg + 1) * 4)));
+        size_t b_off = align256((nseg + 1) * 4);
+        CK(scratch(&s, b_off + ft::segsum_scratch_bytes(src->n)));
         CK(h2d(s, off, (nseg + 1) * 4));
-        CK(ft::segsum(ft::view_of(a), (const int32_t *)s, nseg, ft::view_of(src), src->n, nullptr, 0, g.stream));
+        CK(ft::segsum(ft::view_of(a), (const int32_t *)s, nseg, ft::view_of(src), src->n, nullptr, 0,
+                      (uint8_t *)s + b_off, g.stream));
         return FT_ERR_NO_ERROR;
     });
 }

@@ -72,11 +72,19 @@ int set_ladder_block(int nt);
 // ---- reductions (k_reduce.cu)
 size_t reduce_scratch_bytes(size_t n);
 cudaError_t reduce(View out, View src, size_t n, void *d_scratch, cudaStream_t st);
+// scan: per-thread sums of SCAN_K points, recursively, down to one block
+constexpr size_t SCAN_K = 16;
+constexpr size_t SCAN_SMALL_MAX = 4096;
+constexpr size_t scan_scratch_points(size_t n)
+{
+    return n <= SCAN_SMALL_MAX ? 0 : (n + SCAN_K - 1) / SCAN_K + scan_scratch_points((n + SCAN_K - 1) / SCAN_K);
+}
 size_t scan_scratch_bytes(size_t n);
 cudaError_t scan(View v, size_t n, int exclusive, void *d_scratch, cudaStream_t st);
 // out[s] (+)= sum of src[perm ? perm[e] : e] for e in [off[s], off[s+1])
+size_t segsum_scratch_bytes(size_t nsrc);
 cudaError_t segsum(View out, const int32_t *d_off, size_t nseg, View src, size_t nsrc,
-                   const int32_t *d_perm, int accumulate, cudaStream_t st);
+                   const int32_t *d_perm, int accumulate, void *d_scratch, cudaStream_t st);
 // counting sort of keys < nkeys: d_off (nkeys + 1) and d_perm (n); *d_bad set to
 // the largest out-of-range position, or left at -1
 size_t isum_scratch_bytes(size_t n, size_t nkeys);

@@ -11,7 +11,7 @@
 //
 // Limits and sharing:
 //  * at most FT_NOALLOC_SCAN_MAX_POINTS points per call (FT_ERR_BAD_SIZE
-//    beyond it); the array is FT_NOALLOC_SCAN_SCRATCH_BYTES (about 17 MB) and
+//    beyond it); the array is FT_NOALLOC_SCAN_SCRATCH_BYTES (about 9 MB) and
 //    is resident on every GPU that loads the library until the process exits;
 //  * every call uses the same array and leaves its partial sums there; each
 //    launch writes all scratch it later reads, so nothing must start at zero;
@@ -26,21 +26,9 @@
 #include "../../include/ftcrypto.h"
 #include "../../include/ftcrypto_gb300.h"
 
-// scratch layout of ft::scan at the maximum size: per level, one point per
-// thread of each 1024-point chunk plus one per chunk (see k_reduce.cu)
-static constexpr size_t noalloc_scan_points(size_t n)
-{
-    size_t pts = 0;
-    while (n > 1) {
-        size_t nch = (n + 1023) / 1024;
-        pts += nch * 128 + nch;
-        n = nch;
-    }
-    return pts;
-}
-
+// the scan's scratch at the maximum size (ft::scan_scratch_points)
 static constexpr size_t FT_NOALLOC_SCAN_SCRATCH_BYTES =
-    ((noalloc_scan_points(FT_NOALLOC_SCAN_MAX_POINTS) * 128 + 256 + 255) / 256) * 256;
+    ((ft::scan_scratch_points(FT_NOALLOC_SCAN_MAX_POINTS) * 128 + 256 + 255) / 256) * 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[FT_NOALLOC_SCAN_SCRATCH_BYTES];
 
@@ -75,8 +63,6 @@ extern "C" ft_error ftx_scan_noalloc(void *d_planes, size_t stride, size_t n, in
     if (n > FT_NOALLOC_SCAN_MAX_POINTS) return FT_ERR_BAD_SIZE;
     if (n > stride) return FT_ERR_SIZE_MISMATCH;
     if (n == 0) return FT_ERR_NO_ERROR;
-    static_assert(noalloc_scan_points(FT_NOALLOC_SCAN_MAX_POINTS) * 128 + 256 <= FT_NOALLOC_SCAN_SCRATCH_BYTES,
-                  "scratch covers the largest scan");
     if (ft::scan_scratch_bytes(n) > FT_NOALLOC_SCAN_SCRATCH_BYTES) return FT_ERR_INTERNAL_LIBRARY_ERROR;
     void *scratch = nullptr;
     cudaError_t e = scratch_address(&scratch);

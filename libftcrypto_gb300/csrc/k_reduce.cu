@@ -8,25 +8,25 @@
 //            input point (the reference's tree does the same count but with
 //            most threads idle at the upper levels and 160-byte AoS loads).
 //   scan     inclusive / exclusive prefix (ft_array_scan / ft_array_prescan;
-//            ftcrypto.cu:1474-1586) as reduce-then-scan over chunks of
-//            NT*K points: (A) per-thread sums of K consecutive points and per-
-//            chunk sums, (B) exclusive scan of the chunk sums (recursively),
-//            (C) block scan of the thread sums and a sequential rescan of each
-//            thread's K points.  ~2 + 8/K additions per point and no waits
-//            between blocks.  Correct for every length (the reference's
-//            kernel indexes its tile sums wrongly above 256 x grid points,
-//            ftcrypto.cu:1512).
+//            ftcrypto.cu:1474-1586): per-thread sums of SCAN_K = 16 consecutive
+//            points, an exclusive scan of those sums by the same routine (one
+//            block once at most 4096 remain), then each thread rescans its 16
+//            points from its prefix.  ~2 + 2/16 additions per point, one
+//            point-addition site per kernel, no waits between blocks.  Correct
+//            for every length (the reference's kernel indexes its tile sums
+//            wrongly above 256 x grid points, ftcrypto.cu:1512).
 //   segsum   out[s] = sum of src[e] (or src[perm[e]]) for e in
-//            [off[s], off[s+1]): each block owns a contiguous range of whole
-//            segments; within it, chunks of NT*K points in which every thread
-//            sums its K consecutive points segment by segment, writes the
-//            segments that begin and end inside it, and gets the partial sum
-//            of the segment it starts inside from a block-wide segmented scan
-//            of (has-segment-start, running sum) pairs.  ~1 + 8/K additions
-//            per point.  It serves ft_reduce_isum (ftcrypto.cu:1113-1217,
-//            accumulating into res) and the CSR segmented-sum extension.
+//            [off[s], off[s+1]): each thread sums 16 consecutive points segment
+//            by segment, writes the segments that begin and end inside it and
+//            records the parts of the segments crossing its edges; a second
+//            kernel joins those parts (k_seg_walk / k_seg_join).  ~1 + 1/16
+//            additions per point.  It serves ft_reduce_isum
+//            (ftcrypto.cu:1113-1217, accumulating into res) and the CSR
+//            segmented-sum extension.
 //   keys_to_csr  counting sort of ft_reduce_isum's keys on the device
 //            (replaces the reference's host std::sort, ftcrypto.cu:1170).
+#include <algorithm>
+
 #include "internal.h"
 #include "points.cuh"
 
@@ -128,91 +128,106 @@ FT_DEV void block_scan_excl(ge_p3 &ex, const ge_p3 &x, uint4 *sm /* (NT/32) * 8 
     ge_addto(ex, lex);
 }
 
-// (A) thread sums tt[c*NT + t] of K consecutive points; chunk sums ct[c]
+// per-thread sums of K consecutive points: ts[t] = sum of p[tK .. tK+K)
+template <int K>
+__global__ void __launch_bounds__(128) k_scan_sums(const uint4 *p, size_t s, size_t n, uint4 *ts, size_t tss)
+{
+    const size_t nt = (n + K - 1) / K;
+    FT_GRID_LOOP(t, nt)
+    {
+        const size_t e0 = t * K;
+        ge_p3 acc;
+        ld_p3(acc, p, s, e0);
+#pragma unroll 1
+        for (int k = 1; k < K; ++k) {
+            const size_t e = e0 + k;
+            if (e >= n) break;
+            ge_p3 x;
+            ld_p3(x, p, s, e);
+            ge_addto(acc, x);
+        }
+        st_p3(ts, tss, t, acc);
+    }
+}
+
+// rescan each thread's K points starting from its exclusive prefix ts[t]
+template <int K>
+__global__ void __launch_bounds__(128) k_scan_apply(uint4 *p, size_t s, size_t n, const uint4 *ts, size_t tss,
+                                                    int exclusive)
+{
+    const size_t nt = (n + K - 1) / K;
+    FT_GRID_LOOP(t, nt)
+    {
+        ge_p3 pre;
+        ld_p3(pre, ts, tss, t);
+#pragma unroll 1
+        for (int k = 0; k < K; ++k) {
+            const size_t e = t * K + k;
+            if (e >= n) break;
+            ge_p3 x;
+            ld_p3(x, p, s, e);
+            if (exclusive) st_p3(p, s, e, pre);
+            ge_addto(pre, x);
+            if (!exclusive) st_p3(p, s, e, pre);
+        }
+    }
+}
+
+// one block scans n <= NT * K points in place: thread sums, a block-wide
+// exclusive scan of them, then the sequential rescan
 template <int NT, int K>
-__global__ void __launch_bounds__(NT) k_scan_sums(const uint4 *p, size_t s, size_t n, uint4 *tt, size_t ts,
-                                                  uint4 *ct, size_t cs)
+__global__ void __launch_bounds__(NT) k_scan_small(uint4 *p, size_t s, size_t n, int exclusive)
 {
     __shared__ uint4 sm[(NT / 32) * 8];
-    const size_t c = blockIdx.x;
-    const size_t e0 = c * (size_t)(NT * K) + (size_t)threadIdx.x * K;
+    const size_t e0 = (size_t)threadIdx.x * K;
     ge_p3 acc;
     ge_p3_0(acc);
     if (e0 < n) ld_p3(acc, p, s, e0);
 #pragma unroll 1
     for (int k = 1; k < K; ++k) {
-        size_t e = e0 + k;
+        const size_t e = e0 + k;
         if (e >= n) break;
         ge_p3 x;
         ld_p3(x, p, s, e);
         ge_addto(acc, x);
     }
-    st_p3(tt, ts, c * NT + threadIdx.x, acc);
-    block_sum<NT>(acc, sm);
-    if (threadIdx.x == 0) st_p3(ct, cs, c, acc);
-}
-
-// (C) rescan each thread's K points from its exclusive prefix
-template <int NT, int K>
-__global__ void __launch_bounds__(NT) k_scan_apply(uint4 *p, size_t s, size_t n, const uint4 *tt, size_t ts,
-                                                   const uint4 *ct, size_t cs, int exclusive)
-{
-    __shared__ uint4 sm[(NT / 32) * 8];
-    const size_t c = blockIdx.x;
-    const size_t e0 = c * (size_t)(NT * K) + (size_t)threadIdx.x * K;
-    ge_p3 x, pre;
-    ld_p3(x, tt, ts, c * NT + threadIdx.x);
-    block_scan_excl<NT>(pre, x, sm);
-    ge_p3 cp;
-    ld_p3(cp, ct, cs, c);
-    ge_addto(pre, cp);
+    ge_p3 pre;
+    block_scan_excl<NT>(pre, acc, sm);
 #pragma unroll 1
     for (int k = 0; k < K; ++k) {
-        size_t e = e0 + k;
+        const size_t e = e0 + k;
         if (e >= n) break;
+        ge_p3 x;
         ld_p3(x, p, s, e);
-        if (exclusive) {
-            st_p3(p, s, e, pre);
-            ge_addto(pre, x);
-        } else {
-            ge_addto(pre, x);
-            st_p3(p, s, e, pre);
-        }
+        if (exclusive) st_p3(p, s, e, pre);
+        ge_addto(pre, x);
+        if (!exclusive) st_p3(p, s, e, pre);
     }
 }
 
-static const int SCAN_NT = 128, SCAN_K = 8;
-static const size_t SCAN_CHUNK = (size_t)SCAN_NT * SCAN_K;
+static const int SMALL_NT = 256;
 
-size_t scan_scratch_bytes(size_t n)
-{
-    size_t pts = 0;
-    while (n > 1) {
-        size_t nch = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
-        pts += nch * SCAN_NT + nch;
-        n = nch;
-    }
-    return pts * 128 + 256;
-}
+size_t scan_scratch_bytes(size_t n) { return scan_scratch_points(n) * 128 + 256; }
 
+// thread sums of SCAN_K points, an exclusive scan of those sums (the same
+// routine on an array SCAN_K times shorter, until one block suffices), then
+// the rescan: about 2 + 2/SCAN_K additions per point, no waits between blocks
 cudaError_t scan(View v, size_t n, int exclusive, void *scratch, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
-    size_t nch = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
-    View tt{(uint4 *)scratch, nch * SCAN_NT};
-    View ct{tt.p + FT_PLANES * tt.s, nch};
-    void *rest = ct.p + FT_PLANES * ct.s;
-    k_scan_sums<SCAN_NT, SCAN_K><<<(unsigned)nch, SCAN_NT, 0, st>>>(v.p, v.s, n, tt.p, tt.s, ct.p, ct.s);
+    if (n <= SCAN_SMALL_MAX) {
+        k_scan_small<SMALL_NT, SCAN_SMALL_MAX / SMALL_NT><<<1, SMALL_NT, 0, st>>>(v.p, v.s, n, exclusive);
+        return cudaGetLastError();
+    }
+    const size_t nt = (n + SCAN_K - 1) / SCAN_K;
+    View ts{(uint4 *)scratch, nt};
+    void *rest = ts.p + FT_PLANES * nt;
+    const unsigned grid = (unsigned)((nt + 127) / 128);
+    k_scan_sums<SCAN_K><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    if (nch > 1) {
-        e = scan(ct, nch, 1, rest, st);
-        if (e != cudaSuccess) return e;
-    } else {
-        e = set_zero(ct, 1, st);
-        if (e != cudaSuccess) return e;
-    }
-    k_scan_apply<SCAN_NT, SCAN_K><<<(unsigned)nch, SCAN_NT, 0, st>>>(v.p, v.s, n, tt.p, tt.s, ct.p, ct.s, exclusive);
+    if ((e = scan(ts, nt, 1, rest, st)) != cudaSuccess) return e;
+    k_scan_apply<SCAN_K><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s, exclusive);
     return cudaGetLastError();
 }
 
@@ -247,25 +262,6 @@ cudaError_t reduce(View out, View src, size_t n, void *scratch, cudaStream_t st)
 
 // ------------------------------------------------------------ segmented sum
 
-// segmented combine: (f1, v1) then (f2, v2) -> (f1 | f2, f2 ? v2 : v1 + v2)
-FT_DEV void seg_combine(int &f, ge_p3 &v, int f_prev, const ge_p3 &v_prev)
-{
-    ge_p3 sum = v_prev;
-    ge_addto(sum, v);
-    if (!f) v = sum;
-    f |= f_prev;
-}
-
-FT_DEV int lower_bound_i32(const int32_t *a, int lo, int hi, long long x) // first i in [lo,hi) with a[i] >= x
-{
-    while (lo < hi) {
-        int mid = lo + ((hi - lo) >> 1);
-        if ((long long)a[mid] < x) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
 FT_DEV int upper_bound_i32(const int32_t *a, int lo, int hi, long long x) // first i in [lo,hi) with a[i] > x
 {
     while (lo < hi) {
@@ -276,199 +272,137 @@ FT_DEV int upper_bound_i32(const int32_t *a, int lo, int hi, long long x) // fir
     return lo;
 }
 
-template <int NT, int K>
-__global__ void __launch_bounds__(NT) k_segsum(uint4 *op, size_t os, const int32_t *off, int nseg, const uint4 *sp,
-                                               size_t ss, long long nsrc, const int32_t *perm, int accumulate)
+FT_DEV void seg_write(uint4 *op, size_t os, int sg, const ge_p3 &v, int accumulate)
 {
-    constexpr int NW = NT / 32;
-    __shared__ uint4 s_wv[NW * 8];
-    __shared__ int s_wf[NW];
-    __shared__ uint4 s_carry[8];
-    __shared__ int s_cf;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long G = gridDim.x, b = blockIdx.x;
-
-    // this block's whole segments [s0, s1) and their points [E0, E1)
-    const int s0 = b == 0 ? 0 : lower_bound_i32(off, 0, nseg + 1, nsrc * b / G);
-    const int s1 = b == G - 1 ? nseg : lower_bound_i32(off, 0, nseg + 1, nsrc * (b + 1) / G);
-    if (s0 >= s1) return;
-    const long long E0 = off[s0], E1 = off[s1];
-
-    // empty segments produce the identity (or leave res untouched)
-    if (!accumulate) {
-        for (int sg = s0 + threadIdx.x; sg < s1; sg += NT) {
-            if (off[sg] == off[sg + 1]) {
-                ge_p3 z;
-                ge_p3_0(z);
-                st_p3(op, os, sg, z);
-            }
-        }
-    }
-    if (threadIdx.x == 0) {
-        ge_p3 z;
-        ge_p3_0(z);
-        sm_st_p3(s_carry, 0, z);
-        s_cf = 0;
-    }
-    __syncthreads();
-
-#pragma unroll 1
-    for (long long c0 = E0; c0 < E1; c0 += (long long)NT * K) {
-        const long long cend = min(E1, c0 + (long long)NT * K);
-        const long long e0 = c0 + (long long)threadIdx.x * K;
-        // pass 1: walk this thread's points
-        int fstart = 0, head_pending = 0, head_seg = 0, any = 0, open_before = 1;
-        ge_p3 acc, head;
-        ge_p3_0(acc);
-        ge_p3_0(head);
-        if (e0 < cend) {
-            int sg = upper_bound_i32(off, s0, s1 + 1, e0) - 1;
-#pragma unroll 1
-            for (int k = 0; k < K; ++k) {
-                const long long e = e0 + k;
-                if (e >= cend) break;
-                while ((long long)off[sg + 1] <= e) ++sg;
-                ge_p3 x;
-                ld_p3(x, sp, ss, perm ? (size_t)perm[e] : (size_t)e);
-                if ((long long)off[sg] == e) {
-                    fstart = 1;
-                    open_before = 0;
-                    acc = x;
-                } else if (!any) {
-                    acc = x;
-                } else {
-                    ge_addto(acc, x);
-                }
-                any = 1;
-                if ((long long)off[sg + 1] == e + 1) { // last point of segment sg
-                    if (open_before) {
-                        head = acc;
-                        head_pending = 1;
-                        head_seg = sg;
-                        open_before = 0;
-                    } else {
-                        ge_p3 o = acc;
-                        if (accumulate) {
-                            ge_p3 r;
-                            ld_p3(r, op, os, sg);
-                            ge_addto(r, o);
-                            o = r;
-                        }
-                        st_p3(op, os, sg, o);
-                    }
-                }
-            }
-        }
-        // block-wide exclusive segmented scan of (fstart, acc), seeded by the
-        // carry from the previous chunk
-        int f = fstart;
-        ge_p3 v = acc;
-#pragma unroll 1
-        for (int o = 1; o < 32; o <<= 1) {
-            ge_p3 vu;
-            shfl_up_p3(vu, v, o);
-            int fu = __shfl_up_sync(0xffffffffu, f, o);
-            int f2 = f;
-            ge_p3 v2 = v;
-            seg_combine(f2, v2, fu, vu);
-            if (lane >= o) {
-                f = f2;
-                v = v2;
-            }
-        }
-        if (lane == 31) {
-            sm_st_p3(s_wv, warp, v);
-            s_wf[warp] = f;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            // scan of [carry, warp totals...]; lane w ends with the prefix of warp w
-            int wf = 0;
-            ge_p3 wv;
-            ge_p3_0(wv);
-            if (lane < NW) {
-                sm_ld_p3(wv, s_wv, lane);
-                wf = s_wf[lane];
-            }
-#pragma unroll 1
-            for (int o = 1; o < 32; o <<= 1) {
-                ge_p3 vu;
-                shfl_up_p3(vu, wv, o);
-                int fu = __shfl_up_sync(0xffffffffu, wf, o);
-                int f2 = wf;
-                ge_p3 v2 = wv;
-                seg_combine(f2, v2, fu, vu);
-                if (lane >= o) {
-                    wf = f2;
-                    wv = v2;
-                }
-            }
-            // exclusive prefix of warp w = carry (+) inclusive of warps < w
-            ge_p3 ex;
-            shfl_up_p3(ex, wv, 1);
-            int exf = __shfl_up_sync(0xffffffffu, wf, 1);
-            ge_p3 cv;
-            sm_ld_p3(cv, s_carry, 0);
-            int cf = s_cf;
-            if (lane == 0) {
-                ex = cv;
-                exf = cf;
-            } else {
-                seg_combine(exf, ex, cf, cv);
-            }
-            // new carry = carry (+) all warps
-            ge_p3 tot = wv;
-            int totf = wf;
-            seg_combine(totf, tot, cf, cv);
-            __syncwarp();
-            if (lane < NW) {
-                sm_st_p3(s_wv, lane, ex);
-                s_wf[lane] = exf;
-            }
-            if (lane == NW - 1) {
-                sm_st_p3(s_carry, 0, tot);
-                s_cf = totf;
-            }
-        }
-        __syncthreads();
-        // carry into this thread = warp prefix (+) lanes before it
-        ge_p3 lv;
-        shfl_up_p3(lv, v, 1);
-        int lf = __shfl_up_sync(0xffffffffu, f, 1);
-        ge_p3 cin;
-        sm_ld_p3(cin, s_wv, warp);
-        int cinf = s_wf[warp];
-        if (lane > 0) {
-            seg_combine(lf, lv, cinf, cin);
-            cin = lv;
-        }
-        if (head_pending) {
-            ge_addto(cin, head);
-            if (accumulate) {
-                ge_p3 r;
-                ld_p3(r, op, os, head_seg);
-                ge_addto(r, cin);
-                cin = r;
-            }
-            st_p3(op, os, head_seg, cin);
-        }
-        __syncthreads(); // s_wv and the carry are rewritten next chunk
+    if (accumulate) {
+        ge_p3 r;
+        ld_p3(r, op, os, sg);
+        ge_addto(r, v);
+        st_p3(op, os, sg, r);
+    } else {
+        st_p3(op, os, sg, v);
     }
 }
 
-static const int SEG_NT = 128, SEG_K = 16;
+// record flags of a thread in the segmented sum
+#define SEG_HEAD 1u   // H[t] holds the part of a segment that began before the thread
+#define SEG_CLOSE 2u  // ... and that segment ends inside the thread (or at its last point)
+#define SEG_TAIL 4u   // L[t] holds the start of segment lseg[t], which continues past the thread
 
+// Pass 1: thread t sums its K consecutive points segment by segment.  A
+// segment that begins and ends inside the thread is written at once; the
+// parts of segments crossing the thread's edges go to H / L.
+template <int K>
+__global__ void __launch_bounds__(128) k_seg_walk(uint4 *op, size_t os, const int32_t *off, int nseg, const uint4 *sp,
+                                                  size_t ss, long long nsrc, const int32_t *perm, int accumulate,
+                                                  uint4 *H, uint4 *Lp, size_t hs, uint32_t *flags, int32_t *lseg)
+{
+    const long long nt = (nsrc + K - 1) / K;
+    FT_GRID_LOOP(t, (size_t)nt)
+    {
+        const long long e0 = (long long)t * K;
+        const long long e1 = min(e0 + K, nsrc);
+        int sg = upper_bound_i32(off, 0, nseg + 1, e0) - 1; // segment holding e0 (skips empty ones)
+        bool open_before = (long long)off[sg] < e0;
+        uint32_t fl = 0;
+        ge_p3 acc;
+        ge_p3_0(acc);
+#pragma unroll 1
+        for (long long e = e0; e < e1; ++e) {
+            while ((long long)off[sg + 1] <= e) ++sg;
+            ge_p3 x;
+            ld_p3(x, sp, ss, perm ? (size_t)perm[e] : (size_t)e);
+            if ((long long)off[sg] == e || e == e0) acc = x;
+            else ge_addto(acc, x);
+            if ((long long)off[sg + 1] == e + 1) { // last point of segment sg
+                if (open_before) {
+                    st_p3(H, hs, t, acc);
+                    fl |= SEG_HEAD | SEG_CLOSE;
+                    open_before = false;
+                } else {
+                    seg_write(op, os, sg, acc, accumulate);
+                }
+            }
+        }
+        if ((long long)off[sg + 1] > e1) { // the last segment continues past the thread
+            if (open_before) {
+                st_p3(H, hs, t, acc);
+                fl |= SEG_HEAD;
+            } else {
+                st_p3(Lp, hs, t, acc);
+                fl |= SEG_TAIL;
+                lseg[t] = sg;
+            }
+        }
+        flags[t] = fl;
+    }
+}
+
+// Pass 2: a segment started in thread t and continuing past it totals
+// L[t] + H[t+1] + ... + H[u], u the first later thread whose head closes it.
+__global__ void __launch_bounds__(128) k_seg_join(uint4 *op, size_t os, const uint4 *H, const uint4 *Lp, size_t hs,
+                                                  const uint32_t *flags, const int32_t *lseg, size_t nt, int accumulate)
+{
+    FT_GRID_LOOP(t, nt)
+    {
+        if (!(flags[t] & SEG_TAIL)) continue;
+        ge_p3 sum;
+        ld_p3(sum, Lp, hs, t);
+#pragma unroll 1
+        for (size_t u = t + 1; u < nt; ++u) {
+            ge_p3 h;
+            ld_p3(h, H, hs, u);
+            ge_addto(sum, h);
+            if (flags[u] & SEG_CLOSE) break;
+        }
+        seg_write(op, os, lseg[t], sum, accumulate);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_seg_empty(uint4 *op, size_t os, const int32_t *off, size_t nseg)
+{
+    FT_GRID_LOOP(sg, nseg)
+    {
+        if (off[sg] == off[sg + 1]) {
+            ge_p3 z;
+            ge_p3_0(z);
+            st_p3(op, os, sg, z);
+        }
+    }
+}
+
+static const int SEG_K = 16;
+
+size_t segsum_scratch_bytes(size_t nsrc)
+{
+    size_t nt = (nsrc + SEG_K - 1) / SEG_K;
+    return 2 * nt * 128 + 2 * nt * 4 + 1024;
+}
+
+// out[s] (+)= sum of src[perm ? perm[e] : e], e in [off[s], off[s+1]):
+// ~1 + 1/SEG_K additions per point, two kernels, no waits between blocks.
+// A segment spanning m threads costs m sequential additions in pass 2
+// (m ~ length / 16; about 1-3 for the benchmark's mean lengths 8-32).
 cudaError_t segsum(View out, const int32_t *off, size_t nseg, View src, size_t nsrc, const int32_t *perm,
-                   int accumulate, cudaStream_t st)
+                   int accumulate, void *scratch, cudaStream_t st)
 {
     if (nseg == 0) return cudaSuccess;
-    size_t per_block = (size_t)SEG_NT * SEG_K * 8;
-    size_t g = (nsrc + per_block - 1) / per_block;
-    size_t cap = (size_t)sm_count() * 6;
-    if (g > cap) g = cap;
-    if (g == 0) g = 1;
-    k_segsum<SEG_NT, SEG_K><<<(unsigned)g, SEG_NT, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s,
-                                                             (long long)nsrc, perm, accumulate);
+    cudaError_t e;
+    if (!accumulate) {
+        k_seg_empty<<<(unsigned)std::min<size_t>((nseg + 255) / 256, 65535), 256, 0, st>>>(out.p, out.s, off, nseg);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if (nsrc == 0) return cudaSuccess;
+    const size_t nt = (nsrc + SEG_K - 1) / SEG_K;
+    uint4 *H = (uint4 *)scratch;
+    uint4 *Lp = H + FT_PLANES * nt;
+    uint32_t *flags = (uint32_t *)(Lp + FT_PLANES * nt);
+    int32_t *lseg = (int32_t *)(flags + nt);
+    const unsigned grid = (unsigned)((nt + 127) / 128);
+    k_seg_walk<SEG_K><<<grid, 128, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s, (long long)nsrc, perm,
+                                             accumulate, H, Lp, nt, flags, lseg);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_seg_join<<<grid, 128, 0, st>>>(out.p, out.s, H, Lp, nt, flags, lseg, nt, accumulate);
     return cudaGetLastError();
 }
 
