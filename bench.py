@@ -390,7 +390,96 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     ms = timed(ev, lambda: (t1.scan(), t2.scan()), 3)
     out["scan_4M_ct"] = {"ct_per_s": n4 / (ms * 1e-3), "ms": ms, "decrypt_check_sample": ok,
                          **roof(2 * n4 * 2 * B_PT, 2 * n4 * 9 * 64, ms, hbm_peak, imad)}
+    del c1, c2, t1, t2
+    out["batched_uneven_4096"] = uneven_batch(ft, synth, torch, st)
     return out
+
+
+def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=3):
+    """4,096 ciphertext arrays, lengths log-uniform in [1, 65,536], each with
+    one op (add 40%, scale by k in [1,1000] 30%, segmented sum of mean-8
+    segments 30%): one persistent launch replayed from a CUDA graph against
+    one library call per array (ft_add / ftx_scale_small /
+    ftx_segmented_sum_csr_device, two per ciphertext array)."""
+    ev = Ev(st)
+    g = synth.rng(SEED + 11)
+    work = synth.uneven_mix(g, n_arrays=n_arrays)
+    pool = 1 << 17
+    base = ft.Array.from_scalars(synth.scalars_mod_L(g, pool))
+    arrs, dev_off = [], []
+    for w in work:
+        n = w["len"]
+        o = int(g.integers(0, pool - n + 1))
+        c1, c2 = base.get_range(o, o + n, 1), base.get_range(pool - n - o, pool - o, 1)
+        ex = {}
+        if w["op"] == "add":
+            ex["s1"], ex["s2"] = base.get_range(0, n, 1), base.get_range(pool - n, pool, 1)
+        elif w["op"] == "segsum":
+            nseg = len(w["offsets"]) - 1
+            ex["o1"], ex["o2"] = ft.Array.init_scalar(nseg), ft.Array.init_scalar(nseg)
+            ex["doff"] = torch.from_numpy(w["offsets"]).cuda()
+        arrs.append((c1, c2, ex))
+    torch.cuda.synchronize()
+
+    def plain(sub=None):
+        for w, (c1, c2, ex) in (sub or list(zip(work, arrs))):
+            if w["op"] == "add":
+                c1.add(ex["s1"])
+                c2.add(ex["s2"])
+            elif w["op"] == "scale":
+                c1.scale_small(w["k"])
+                c2.scale_small(w["k"])
+            else:
+                nseg = len(ex["o1"])
+                ft.segmented_sum_csr_device(ex["o1"], ex["doff"].data_ptr(), nseg, c1)
+                ft.segmented_sum_csr_device(ex["o2"], ex["doff"].data_ptr(), nseg, c2)
+
+    def batch_of(pairs):
+        b = ft.Batch()
+        for w, (c1, c2, ex) in pairs:
+            if w["op"] == "add":
+                b.add(c1, ex["s1"])
+                b.add(c2, ex["s2"])
+            elif w["op"] == "scale":
+                b.scale_small(c1, w["k"])
+                b.scale_small(c2, w["k"])
+            else:
+                b.segmented_sum(ex["o1"], w["offsets"], c1)
+                b.segmented_sum(ex["o2"], w["offsets"], c2)
+        return b
+
+    # bit-exact: both forms on copies of the first 256 arrays
+    def cp(a):
+        return a.get_range(0, len(a), 1)
+    sub = list(zip(work, arrs))[:256]
+    s_plain = [(w, (cp(c1), cp(c2), {k: (cp(v) if k != "doff" else v) for k, v in ex.items()})) for w, (c1, c2, ex) in sub]
+    s_batch = [(w, (cp(c1), cp(c2), {k: (cp(v) if k != "doff" else v) for k, v in ex.items()})) for w, (c1, c2, ex) in sub]
+    plain(s_plain)
+    sb = batch_of(s_batch)
+    sb.run()
+
+    def outs(pairs):
+        r = []
+        for w, (c1, c2, ex) in pairs:
+            r += [ex["o1"], ex["o2"]] if w["op"] == "segsum" else [c1, c2]
+        return r
+    same = all((x.to_bytes_folded() == y.to_bytes_folded()).all() for x, y in zip(outs(s_plain), outs(s_batch)))
+    sb.free()
+    del s_plain, s_batch
+
+    b = batch_of(list(zip(work, arrs)))
+    b.run()  # uploads the work list and captures the graph
+    ft.synchronize()
+    ms_batch = timed(ev, b.run, reps)
+    plain()
+    ft.synchronize()
+    ms_plain = timed(ev, plain, reps)
+    n_items, n_ops = b.info()
+    n_ct = int(sum(w["len"] for w in work))
+    return {"arrays": n_arrays, "ciphertexts": n_ct, "ops": n_ops, "work_items": n_items,
+            "batched_graph_ms": ms_batch, "plain_per_array_ms": ms_plain, "speedup": ms_plain / ms_batch,
+            "batched_ct_per_s": n_ct / (ms_batch * 1e-3), "bit_exact_batched_vs_plain_256_arrays": bool(same),
+            "launches": {"batched": 1, "plain": 2 * n_arrays}}
 
 
 # ---------------------------------------------------------------- CPU side

@@ -68,10 +68,41 @@ ft_error ftx_segmented_sum_csr_device(ft_ge25519_array out, const int32_t *d_off
 /* out[out_idx] = sum of src, leaving src unchanged. */
 ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_array src);
 
+/* a[i] = k * a[i] for a public bound k < 2^32, constant time in k: nine
+ * radix-16 windows of the reference's ladder instead of 64 (same points as
+ * ft_scale with the 32-byte scalar k). */
+ft_error ftx_scale_small(ft_ge25519_array array, uint32_t k);
+
+/* Batched form: record many independent operations on arrays of any
+ * lengths, then run them all in one persistent kernel launch replayed from a
+ * CUDA graph.  The first ftx_batch_run uploads the work list and captures
+ * the graph; later runs replay it (re-running every operation on the arrays'
+ * current contents).  Operations of one batch run concurrently: an array
+ * written by one operation must not appear in any other operation of the
+ * batch (FT_ERR_BAD_SIZE at record time otherwise).  Arrays must stay
+ * allocated and keep their length while the batch exists; recording after
+ * the first run returns FT_ERR_BAD_SIZE. */
+struct ftx_batch_s;
+typedef struct ftx_batch_s *ftx_batch;
+ft_error ftx_batch_create(ftx_batch *batch);
+/* res[i] += summand[i] */
+ft_error ftx_batch_add(ftx_batch batch, ft_ge25519_array res, const_ft_ge25519_array summand);
+/* array[i] = k * array[i], k < 2^32 (as ftx_scale_small) */
+ft_error ftx_batch_scale_small(ftx_batch batch, ft_ge25519_array array, uint32_t k);
+/* out[s] = sum of src[offsets[s] .. offsets[s+1]) for s < nseg; out has
+ * length nseg; offsets (host, copied) as for ftx_segmented_sum_csr */
+ft_error ftx_batch_segmented_sum(ftx_batch batch, ft_ge25519_array out, const int32_t *offsets, size_t nseg,
+                                 const_ft_ge25519_array src);
+ft_error ftx_batch_run(ftx_batch batch);
+/* number of work items and of operations recorded */
+ft_error ftx_batch_info(ftx_batch batch, size_t *n_items, size_t *n_ops);
+void ftx_batch_free(ftx_batch batch);
+
 /* Launch-shape knobs, set by the autotuner (libftcrypto_gb300/autotune.py)
  * or by hand.  ftx_tune returns FT_ERR_BAD_SIZE for an unsupported value;
  * ftx_tune_get returns the current value (-1 for an unknown knob). */
-#define FTX_TUNE_LADDER_BLOCK 1 /* variable-base ladder block size: 128, 192 or 224 */
+#define FTX_TUNE_LADDER_BLOCK 1  /* variable-base ladder block size: 128, 192 or 224 */
+#define FTX_TUNE_BATCH_ADD_PTS 2 /* batched form: points per thread of an ADD item (1..64) */
 ft_error ftx_tune(int knob, int value);
 int ftx_tune_get(int knob);
 

@@ -234,6 +234,9 @@ class Array:
         s = _buf(scalars, np.uint8, 32)
         check(lib().ft_mul(self._h, _ptr(s), s.shape[0]))
 
+    def scale_small(self, k: int) -> None:
+        check(lib().ftx_scale_small(self._h, int(k)))
+
     def mul_device(self, d_scalars_ptr: int, n: int) -> None:
         check(lib().ftx_mul_device(self._h, ctypes.c_void_p(d_scalars_ptr), n))
 
@@ -299,3 +302,57 @@ def segmented_sum_csr(offsets, src: Array) -> Array:
 
 def segmented_sum_csr_device(out: Array, d_offsets: int, nseg: int, src: Array) -> None:
     check(lib().ftx_segmented_sum_csr_device(out.handle, ctypes.c_void_p(d_offsets), nseg, src.handle))
+
+
+class Batch:
+    """ftx_batch: many independent array operations in one persistent launch
+    replayed from a CUDA graph.  Keeps references to its arrays."""
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(lib().ftx_batch_create(ctypes.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def add(self, res: Array, summand: Array) -> None:
+        check(lib().ftx_batch_add(self._h, res.handle, summand.handle))
+        self._keep += [res, summand]
+
+    def scale_small(self, arr: Array, k: int) -> None:
+        check(lib().ftx_batch_scale_small(self._h, arr.handle, int(k)))
+        self._keep.append(arr)
+
+    def segmented_sum(self, out: Array, offsets, src: Array) -> None:
+        off = _buf(offsets, np.int32)
+        check(lib().ftx_batch_segmented_sum(self._h, out.handle, _ptr(off), off.size - 1, src.handle))
+        self._keep += [out, src]
+
+    def run(self) -> None:
+        check(lib().ftx_batch_run(self._h))
+
+    def info(self):
+        a, b = ctypes.c_size_t(), ctypes.c_size_t()
+        check(lib().ftx_batch_info(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def free(self) -> None:
+        if self._h:
+            lib().ftx_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.ftx_batch_free(self._h)
+            self._h = None
+
+
+def tune(knob: int, value: int) -> None:
+    check(lib().ftx_tune(knob, value))
+
+
+def tune_get(knob: int) -> int:
+    return int(lib().ftx_tune_get(knob))
+
+
+TUNE_LADDER_BLOCK = 1
+TUNE_BATCH_ADD_PTS = 2

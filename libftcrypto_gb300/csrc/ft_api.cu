@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <set>
 #include <vector>
 
 #include "internal.h"
@@ -894,10 +895,16 @@ ft_error ftx_segmented_sum_csr(ft_ge25519_array *out, const int32_t *off, size_t
     });
 }
 
+static int g_batch_add_pts = 4;
+
 ft_error ftx_tune(int knob, int value)
 {
     switch (knob) {
     case FTX_TUNE_LADDER_BLOCK: return ft::set_ladder_block(value) ? FT_ERR_BAD_SIZE : FT_ERR_NO_ERROR;
+    case FTX_TUNE_BATCH_ADD_PTS:
+        if (value < 1 || value > 64) return FT_ERR_BAD_SIZE;
+        g_batch_add_pts = value;
+        return FT_ERR_NO_ERROR;
     default: return FT_ERR_BAD_SIZE;
     }
 }
@@ -906,6 +913,7 @@ int ftx_tune_get(int knob)
 {
     switch (knob) {
     case FTX_TUNE_LADDER_BLOCK: return ft::ladder_block();
+    case FTX_TUNE_BATCH_ADD_PTS: return g_batch_add_pts;
     default: return -1;
     }
 }
@@ -918,6 +926,185 @@ ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_
     CK(scratch(&s, ft::reduce_scratch_bytes(src->n)));
     CK(ft::reduce(ft::view_of(out, out_idx), ft::view_of(src), src->n, s, g.stream));
     return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_scale_small(ft_ge25519_array array, uint32_t k)
+{
+    ENSURE_INIT();
+    CK(ft::scale_small(ft::view_of(array), array->n, k, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+} // extern "C"
+
+// ---------------------------------------------------------------- batches
+
+struct ftx_batch_s {
+    std::vector<ft::BatchItem> items; // SEG items hold an index into offs in `off` until uploaded
+    std::vector<int32_t> offs;
+    std::set<const void *> written, read;
+    size_t n_ops = 0;
+    ft::BatchItem *d_items = nullptr;
+    int32_t *d_offs = nullptr;
+    int *d_counter = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool ready = false;
+};
+
+namespace {
+
+// an operation writing w and reading r must not touch what other operations
+// of the batch write or read
+ft_error claim(ftx_batch b, const void *w, const void *r)
+{
+    if (b->ready) return FT_ERR_BAD_SIZE;
+    if (w && (b->written.count(w) || b->read.count(w))) return FT_ERR_BAD_SIZE;
+    if (r && r != w && b->written.count(r)) return FT_ERR_BAD_SIZE;
+    if (w) b->written.insert(w);
+    if (r && r != w) b->read.insert(r);
+    b->n_ops++;
+    return FT_ERR_NO_ERROR;
+}
+
+int item_rank(const ft::BatchItem &it)
+{
+    return it.op == ft::BATCH_SCALE ? 0 : (it.op == ft::BATCH_SEG ? 1 : 2);
+}
+
+ft_error batch_upload(ftx_batch b)
+{
+    // costliest kinds first: the persistent blocks finish on short items
+    std::stable_sort(b->items.begin(), b->items.end(),
+                     [](const ft::BatchItem &x, const ft::BatchItem &y) { return item_rank(x) < item_rank(y); });
+    CK(dev_alloc((void **)&b->d_offs, std::max<size_t>(b->offs.size(), 1) * sizeof(int32_t)));
+    for (auto &it : b->items)
+        if (it.op == ft::BATCH_SEG) it.off = b->d_offs + (uintptr_t)it.off;
+    CK(dev_alloc((void **)&b->d_items, std::max<size_t>(b->items.size(), 1) * sizeof(ft::BatchItem)));
+    CK(dev_alloc((void **)&b->d_counter, 256));
+    if (!b->offs.empty())
+        CK(cudaMemcpyAsync(b->d_offs, b->offs.data(), b->offs.size() * 4, cudaMemcpyHostToDevice, g.stream));
+    if (!b->items.empty())
+        CK(cudaMemcpyAsync(b->d_items, b->items.data(), b->items.size() * sizeof(ft::BatchItem),
+                           cudaMemcpyHostToDevice, g.stream));
+    CK(cudaStreamSynchronize(g.stream));
+    CK(ft::batch_prepare());
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t le = ft::batch_launch(b->d_items, (int)b->items.size(), b->d_counter, g.stream);
+    cudaError_t ce = cudaStreamEndCapture(g.stream, &graph);
+    if (le != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return map_err(le);
+    }
+    CK(ce);
+    cudaError_t ie = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ie);
+    b->ready = true;
+    return FT_ERR_NO_ERROR;
+}
+
+} // namespace
+
+extern "C" {
+
+ft_error ftx_batch_create(ftx_batch *batch)
+{
+    ENSURE_INIT();
+    *batch = new (std::nothrow) ftx_batch_s();
+    return *batch ? FT_ERR_NO_ERROR : FT_ERR_OUT_OF_MEMORY;
+}
+
+ft_error ftx_batch_add(ftx_batch b, ft_ge25519_array res, const_ft_ge25519_array summand)
+{
+    if (res->n != summand->n) return FT_ERR_SIZE_MISMATCH;
+    ft_error err = claim(b, res->planes, summand->planes);
+    if (err) return err;
+    const size_t per = (size_t)ft::batch_block() * g_batch_add_pts;
+    for (size_t base = 0; base < res->n; base += per) {
+        ft::BatchItem it{};
+        it.op = ft::BATCH_ADD;
+        it.count = (uint32_t)std::min(per, res->n - base);
+        it.dst = res->planes + base;
+        it.dst_s = res->cap;
+        it.src = summand->planes + base;
+        it.src_s = summand->cap;
+        b->items.push_back(it);
+    }
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_batch_scale_small(ftx_batch b, ft_ge25519_array a, uint32_t k)
+{
+    ft_error err = claim(b, a->planes, nullptr);
+    if (err) return err;
+    const size_t per = (size_t)ft::batch_block();
+    for (size_t base = 0; base < a->n; base += per) {
+        ft::BatchItem it{};
+        it.op = ft::BATCH_SCALE;
+        it.count = (uint32_t)std::min(per, a->n - base);
+        it.dst = a->planes + base;
+        it.dst_s = a->cap;
+        it.k = k;
+        b->items.push_back(it);
+    }
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_batch_segmented_sum(ftx_batch b, ft_ge25519_array out, const int32_t *off, size_t nseg,
+                                 const_ft_ge25519_array src)
+{
+    if (out->n != nseg) return FT_ERR_SIZE_MISMATCH;
+    if (src->n >= (size_t)INT32_MAX || off[0] != 0 || (size_t)off[nseg] != src->n) return FT_ERR_BAD_SIZE;
+    for (size_t s = 0; s < nseg; ++s)
+        if (off[s + 1] < off[s]) return FT_ERR_BAD_SIZE;
+    ft_error err = claim(b, out->planes, src->planes);
+    if (err) return err;
+    const size_t base_off = b->offs.size();
+    b->offs.insert(b->offs.end(), off, off + nseg + 1);
+    const size_t per = (size_t)ft::batch_block();
+    for (size_t s0 = 0; s0 < nseg; s0 += per) {
+        ft::BatchItem it{};
+        it.op = ft::BATCH_SEG;
+        it.count = (uint32_t)std::min(per, nseg - s0);
+        it.dst = out->planes + s0;
+        it.dst_s = out->cap;
+        it.src = src->planes;
+        it.src_s = src->cap;
+        it.off = (const int32_t *)(uintptr_t)(base_off + s0); // patched at upload
+        b->items.push_back(it);
+    }
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_batch_run(ftx_batch b)
+{
+    ENSURE_INIT();
+    if (!b->ready) {
+        ft_error err = batch_upload(b);
+        if (err) return err;
+    }
+    CK(cudaGraphLaunch(b->exec, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_batch_info(ftx_batch b, size_t *n_items, size_t *n_ops)
+{
+    *n_items = b->items.size();
+    *n_ops = b->n_ops;
+    return FT_ERR_NO_ERROR;
+}
+
+void ftx_batch_free(ftx_batch b)
+{
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (g.inited) {
+        dev_free(b->d_items);
+        dev_free(b->d_offs);
+        dev_free(b->d_counter);
+    }
+    delete b;
 }
 
 } // extern "C"

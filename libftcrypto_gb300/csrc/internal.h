@@ -91,6 +91,24 @@ size_t isum_scratch_bytes(size_t n, size_t nkeys);
 cudaError_t keys_to_csr(int32_t *d_off, int32_t *d_perm, const uint64_t *d_keys, size_t n,
                         size_t nkeys, long long *d_bad, void *d_scratch, cudaStream_t st);
 
+// ---- batched form (k_batch.cu)
+enum : uint32_t { BATCH_ADD = 0, BATCH_SCALE = 1, BATCH_SEG = 2 };
+struct BatchItem {
+    uint32_t op;
+    uint32_t count;       // points (ADD, SCALE) or segments (SEG) in this item
+    uint4 *dst;           // planes of the first destination point
+    size_t dst_s;
+    const uint4 *src;     // ADD: summand; SEG: points the offsets index
+    size_t src_s;
+    const int32_t *off;   // SEG: count + 1 offsets into src
+    uint32_t k;           // SCALE: the scalar
+};
+int batch_block();
+size_t batch_smem_bytes();
+cudaError_t batch_prepare(); // once, outside any stream capture
+cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, cudaStream_t st);
+cudaError_t scale_small(View v, size_t n, uint32_t k, cudaStream_t st);
+
 int sm_count();
 
 } // namespace ft

@@ -1,0 +1,121 @@
+// k_batch.cu — the batched form: one persistent kernel for thousands of
+// independent, uneven array operations, and the small-scalar ladder.
+//
+// k_batch: one block per SM (224 threads: the shared-memory ladder tables
+//   of the scale path fill the SM) loops pulling work items from an atomic
+//   counter until the list is exhausted.  Items are pre-sorted costliest
+//   first, so the tail of the run is short ones (longest-processing-time
+//   order).  Item kinds:
+//     ADD    dst[i] += src[i] for count points (count <= 224 x points/thread)
+//     SCALE  dst[i] = k * dst[i], count <= 224 points, one per thread,
+//            constant time in k < 2^32 (smul_ladder_u32)
+//     SEG    dst[s] = sum of src[off[s] .. off[s+1]), count <= 224 segments,
+//            one per thread (segments of the batched workload are short)
+//   The host side (ft_api.cu, ftx_batch_*) captures {counter reset, k_batch}
+//   in a CUDA graph and replays it.
+// k_scale_small: ftx_scale_small, the same small-scalar ladder over one array.
+#include "internal.h"
+#include "ladder.cuh"
+
+namespace ft {
+
+static constexpr int BATCH_NT = 224;
+
+__global__ void __launch_bounds__(BATCH_NT, 1) k_batch(const BatchItem *items, int nitems, int *counter)
+{
+    extern __shared__ uint4 smem[];
+    __shared__ int s_item;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= nitems) break;
+        const BatchItem w = items[it];
+        if (w.op == BATCH_ADD) {
+#pragma unroll 1
+            for (uint32_t e = tid; e < w.count; e += BATCH_NT) {
+                ge_p3 x, y;
+                ld_p3(x, w.dst, w.dst_s, e);
+                ld_p3(y, w.src, w.src_s, e);
+                ge_addto(x, y);
+                st_p3(w.dst, w.dst_s, e, x);
+            }
+        } else if (w.op == BATCH_SCALE) {
+            if ((uint32_t)tid < w.count) {
+                SmemTab<BATCH_NT> tab{smem + tid};
+                ge_p3 P, h;
+                ld_p3(P, w.dst, w.dst_s, tid);
+                smul_build_table(tab, P);
+                smul_ladder_u32(h, w.k, tab);
+                st_p3(w.dst, w.dst_s, tid, h);
+            }
+        } else { // BATCH_SEG
+#pragma unroll 1
+            for (uint32_t sg = tid; sg < w.count; sg += BATCH_NT) {
+                const int32_t a = w.off[sg], b = w.off[sg + 1];
+                ge_p3 acc;
+                ge_p3_0(acc);
+                if (a < b) ld_p3(acc, w.src, w.src_s, a);
+#pragma unroll 1
+                for (int32_t e = a + 1; e < b; ++e) {
+                    ge_p3 x;
+                    ld_p3(x, w.src, w.src_s, e);
+                    ge_addto(acc, x);
+                }
+                st_p3(w.dst, w.dst_s, sg, acc);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BATCH_NT, 1) k_scale_small(uint4 *p, size_t s, size_t n, uint32_t k)
+{
+    extern __shared__ uint4 smem[];
+    const size_t i = (size_t)blockIdx.x * BATCH_NT + threadIdx.x;
+    if (i >= n) return;
+    SmemTab<BATCH_NT> tab{smem + threadIdx.x};
+    ge_p3 P, h;
+    ld_p3(P, p, s, i);
+    smul_build_table(tab, P);
+    smul_ladder_u32(h, k, tab);
+    st_p3(p, s, i, h);
+}
+
+int batch_block() { return BATCH_NT; }
+
+size_t batch_smem_bytes() { return ladder_smem_bytes<BATCH_NT>(); }
+
+static cudaError_t set_smem_attr(const void *f, size_t bytes, bool &done)
+{
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+static bool g_batch_attr = false;
+
+cudaError_t batch_prepare() { return set_smem_attr((const void *)k_batch, batch_smem_bytes(), g_batch_attr); }
+
+cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, cudaStream_t st)
+{
+    cudaError_t e = batch_prepare();
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(d_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
+    k_batch<<<sm_count(), BATCH_NT, batch_smem_bytes(), st>>>(d_items, nitems, d_counter);
+    return cudaGetLastError();
+}
+
+cudaError_t scale_small(View v, size_t n, uint32_t k, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    static bool attr = false;
+    cudaError_t e = set_smem_attr((const void *)k_scale_small, batch_smem_bytes(), attr);
+    if (e != cudaSuccess) return e;
+    k_scale_small<<<(unsigned)((n + BATCH_NT - 1) / BATCH_NT), BATCH_NT, batch_smem_bytes(), st>>>(v.p, v.s, n, k);
+    return cudaGetLastError();
+}
+
+} // namespace ft

@@ -79,6 +79,37 @@ FT_DEV void smul_ladder(ge_p3 &h, const uint32_t a[8], const Tab &tab)
     ge_p1p1_to_p3(h, r);
 }
 
+// h = k * P for k < 2^32, constant time in k: the nine signed radix-16
+// digits a 32-bit scalar has under the reference's recoding (digits 9..63
+// are zero), in the same window sequence as smul_ladder, so the point equals
+// smul_ladder's for the 32-byte scalar k.
+template <class Tab>
+FT_DEV void smul_ladder_u32(ge_p3 &h, uint32_t k, const Tab &tab)
+{
+    const uint64_t b = (uint64_t)k + 0x888888888ull; // nibbles 0..8 biased by 8
+    ge_p3_0(h);
+    ge_p1p1 r;
+    ge_p2 s;
+    ge_cached t;
+    auto get = [&](int j, ge_cached &e) { tab.get(j, e); };
+    int d = (int)((b >> 32) & 15u) - 8;
+#pragma unroll 1
+    for (int i = 8; i > 0; --i) {
+        select_cached(t, d, get);
+        ge_add(r, h, t);
+#pragma unroll 1
+        for (int j = 0; j < 4; ++j) {
+            ge_p1p1_to_p2(s, r);
+            ge_p2_dbl(r, s);
+        }
+        ge_p1p1_to_p3(h, r);
+        d = (int)((b >> (4 * (i - 1))) & 15u) - 8;
+    }
+    select_cached(t, d, get);
+    ge_add(r, h, t);
+    ge_p1p1_to_p3(h, r);
+}
+
 FT_DEV void shr8_256(uint32_t c[8])
 {
 #pragma unroll

@@ -57,6 +57,16 @@ void hc_mul(uint8_t *pts, const uint8_t *scalars, size_t n)
         st(pts + 128 * i, h);
     }
 }
+void hc_mul_u32(uint8_t *pts, const uint32_t *k, size_t n)
+{
+    for (size_t i = 0; i < n; ++i) {
+        ge_p3 p, h; ArrTab tab;
+        ld(p, pts + 128 * i);
+        smul_build_table(tab, p);
+        smul_ladder_u32(h, k[i], tab);
+        st(pts + 128 * i, h);
+    }
+}
 void hc_comb(uint8_t *pts, const uint8_t *scalars, size_t n, int ndigits)
 {
     for (size_t i = 0; i < n; ++i) {

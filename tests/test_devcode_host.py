@@ -98,3 +98,15 @@ def test_decode_and_small_comb(hc, orc):
     c = np.zeros((len(m), 128), np.uint8)
     hc.hc_comb(ptr(c), ptr(small), len(m), 17)
     assert (orc.encode(c) == orc.encode(orc.from_scalars(small))).all()
+
+
+def test_short_ladder_matches_full(hc, orc):
+    g = synth.rng(6)
+    n = 40
+    p = orc.from_scalars(synth.scalars_mod_L(g, n))
+    k = g.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    k[:4] = [0, 1, 2**32 - 1, 1000]
+    m = p.copy()
+    hc.hc_mul_u32(ptr(m), ptr(k), n)
+    full = orc.mul(p, orc.small_to_scalars(k.astype(np.uint64)))
+    assert (orc.encode(m) == orc.encode(full)).all()
