@@ -392,6 +392,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
                          **roof(2 * n4 * 2 * B_PT, 2 * n4 * 9 * 64, ms, hbm_peak, imad)}
     del c1, c2, t1, t2
     out["batched_uneven_4096"] = uneven_batch(ft, synth, torch, st)
+    out["serving"] = serving(ft, synth, torch)
     return out
 
 
@@ -480,6 +481,122 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=3):
             "batched_graph_ms": ms_batch, "plain_per_array_ms": ms_plain, "speedup": ms_plain / ms_batch,
             "batched_ct_per_s": n_ct / (ms_batch * 1e-3), "bit_exact_batched_vs_plain_256_arrays": bool(same),
             "launches": {"batched": 1, "plain": 2 * n_arrays}}
+
+
+def serving(ft, synth, torch, loads=(0.25, 0.5, 0.75, 1.0), n_req=40, budget=120 << 30, slots=8):
+    """Serving: requests of 1,024..4,194,304 ciphertexts (log-uniform), mix
+    35% encrypt of {0,1}, 25% re-randomise, 20% variable-base scalar-mult
+    mod L, 20% segmented sum of mean-32 segments; Poisson arrivals at a
+    fraction of the measured capacity; 120 GB admission budget.  p50 / p99
+    latency (arrival -> GPU work complete) and throughput, for the server
+    (continuous batching over `slots` streams) and for the plain drop-in
+    called once per request on the same arrival schedule."""
+    import threading
+    g = synth.rng(SEED + 21)
+    sk = synth.scalars_mod_L(g, 1)
+    pk = ft.Array.from_scalars(sk).to_bytes_folded()[0]
+    NMAX = 1 << 22
+    r_pool = torch.from_numpy(synth.scalars_mod_L(g, NMAX)).pin_memory().numpy()
+    k_pool = torch.from_numpy(synth.scalars_mod_L(g, NMAX)).pin_memory().numpy()
+    m_pool = torch.from_numpy(to_i64(synth.plaintexts(g, NMAX, 1))).pin_memory().numpy().view(np.uint64)
+    c_pool = ft.encrypt(pk, m_pool, r_pool, 1)
+    ops = ("encrypt", "rerand", "smul", "segsum")
+
+    def make_reqs(n):
+        out = []
+        for _ in range(n):
+            op = ops[int(g.choice(4, p=[0.35, 0.25, 0.2, 0.2]))]
+            size = int(np.floor(np.exp(g.uniform(np.log(1024), np.log(NMAX)))))
+            o = int(g.integers(0, NMAX - size + 1))
+            req = {"op": op, "n": size, "o": o}
+            if op in ("rerand", "smul", "segsum"):
+                req["c"] = (c_pool[0].get_range(o, o + size, 1), c_pool[1].get_range(o, o + size, 1))
+            if op == "segsum":
+                req["off"] = synth.csr_offsets(g, size, max(1, size // 32))
+            out.append(req)
+        ft.synchronize()
+        return out
+
+    def submit(srv, q):
+        n, o = q["n"], q["o"]
+        if q["op"] == "encrypt":
+            return srv.submit_encrypt(m_pool[o:o + n], r_pool[o:o + n], 1)
+        if q["op"] == "rerand":
+            return srv.submit_rerand(*q["c"], r_pool[o:o + n])
+        if q["op"] == "smul":
+            return srv.submit_smul(*q["c"], k_pool[o:o + n])
+        return srv.submit_segsum(*q["c"], q["off"])
+
+    def run_server(reqs, rate):
+        srv = ft.Server(pk, budget, slots)
+        arrivals = np.cumsum(g.exponential(1.0 / rate, len(reqs))) if rate else np.zeros(len(reqs))
+        tickets, lat = [], []
+        done = threading.Event()
+
+        def waiter():
+            for i in range(len(reqs)):
+                while len(tickets) <= i:
+                    time.sleep(0.0001)
+                c1, c2, _, ms = srv.wait(tickets[i])
+                lat.append(ms)
+            done.set()
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        for q, a in zip(reqs, arrivals):
+            d = t0 + a - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tickets.append(submit(srv, q))
+        done.wait()
+        wall = time.perf_counter() - t0
+        th.join()
+        srv.close()
+        return np.array(lat), wall
+
+    def run_plain(reqs, rate):
+        arrivals = np.cumsum(g.exponential(1.0 / rate, len(reqs)))
+        lat = []
+        t0 = time.perf_counter()
+        for q, a in zip(reqs, arrivals):
+            d = t0 + a - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            n, o = q["n"], q["o"]
+            if q["op"] == "encrypt":
+                out = ft.encrypt(pk, m_pool[o:o + n], r_pool[o:o + n], 1)
+            elif q["op"] == "rerand":
+                z = ft.encrypt(pk, np.zeros(n, np.uint64), r_pool[o:o + n], 1)
+                q["c"][0].add(z[0])
+                q["c"][1].add(z[1])
+            elif q["op"] == "smul":
+                q["c"][0].mul(k_pool[o:o + n])
+                q["c"][1].mul(k_pool[o:o + n])
+            else:
+                out = (ft.segmented_sum_csr(q["off"], q["c"][0]), ft.segmented_sum_csr(q["off"], q["c"][1]))
+            ft.synchronize()
+            lat.append((time.perf_counter() - (t0 + a)) * 1e3)
+        return np.array(lat), time.perf_counter() - t0
+
+    # capacity: every request submitted at once
+    reqs = make_reqs(n_req)
+    _, wall = run_server(reqs, 0)
+    capacity = n_req / wall
+    out = {"capacity_req_per_s": capacity, "slots": slots, "budget_gb": budget / 2**30, "requests_per_level": n_req,
+           "levels": []}
+    for load in loads:
+        reqs = make_reqs(n_req)
+        ct = sum(q["n"] for q in reqs)
+        ls, ws = run_server(reqs, load * capacity)
+        lp, wp = run_plain(reqs, load * capacity)
+        out["levels"].append({
+            "offered_load": load, "offered_req_per_s": load * capacity,
+            "server": {"p50_ms": float(np.percentile(ls, 50)), "p99_ms": float(np.percentile(ls, 99)),
+                       "req_per_s": n_req / ws, "ct_per_s": ct / ws},
+            "plain_per_request": {"p50_ms": float(np.percentile(lp, 50)), "p99_ms": float(np.percentile(lp, 99)),
+                                  "req_per_s": n_req / wp, "ct_per_s": ct / wp}})
+        del reqs
+    return out
 
 
 # ---------------------------------------------------------------- CPU side
@@ -671,9 +788,20 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--profile", choices=PROFILE_CASES, help="run one kernel family once, for ncu")
+    ap.add_argument("--serving-sweep", action="store_true",
+                    help="only the serving sweep, offered load 10%%..100%% of capacity in 10%% steps")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args.profile)
+    if args.serving_sweep:
+        import torch
+        import libftcrypto_gb300 as ft
+        from libftcrypto_gb300 import synth
+        ft.build()
+        ft.init()
+        res = serving(ft, synth, torch, loads=tuple(x / 10 for x in range(1, 11)), n_req=40)
+        print(json.dumps({"serving_sweep": res}))
+        return 0
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -98,6 +98,50 @@ ft_error ftx_batch_run(ftx_batch batch);
 ft_error ftx_batch_info(ftx_batch batch, size_t *n_items, size_t *n_ops);
 void ftx_batch_free(ftx_batch batch);
 
+/* Serving form: a request loop with continuous batching.  A server owns a
+ * public key, a budget of device memory and `slots` CUDA streams.  Requests
+ * are queued by ftx_server_submit from any thread and admitted in arrival
+ * order as soon as a slot is free and their device memory (outputs, staged
+ * inputs, scratch) fits in the budget; admitted requests run concurrently,
+ * so work of requests arriving while others are on the GPU overlaps with
+ * theirs.  Ciphertexts stay on the device as handles: ENCRYPT and SEGSUM
+ * create new arrays (the caller frees them with ft_array_free), RERAND and
+ * SMUL update the given arrays in place.  Host buffers named in a request
+ * must stay valid until its result is returned; arrays of a request must not
+ * be used elsewhere until then.  Results are bit-identical to the same
+ * request run alone. */
+#define FTX_REQ_ENCRYPT 1 /* (c1, c2) = Enc(m; r): n plaintexts < 2^bits, n nonces */
+#define FTX_REQ_RERAND 2  /* (c1, c2) += Enc(0; r) */
+#define FTX_REQ_SMUL 3    /* (c1, c2) = k_i * (c1, c2), n 32-byte scalars, constant time */
+#define FTX_REQ_SEGSUM 4  /* new (c1, c2) of nseg segment sums of the given arrays */
+typedef struct {
+    int op;
+    size_t n;                /* ciphertexts */
+    const uint64_t *m;       /* ENCRYPT */
+    unsigned plaintext_bits; /* ENCRYPT */
+    const uint8_t *r;        /* ENCRYPT, RERAND: n x 32 bytes */
+    const uint8_t *k;        /* SMUL: n x 32 bytes */
+    const int32_t *offsets;  /* SEGSUM: nseg + 1 offsets */
+    size_t nseg;             /* SEGSUM */
+    ft_ge25519_array c1, c2; /* RERAND, SMUL (updated); SEGSUM (source) */
+} ftx_request;
+typedef struct {
+    ft_error err;
+    ft_ge25519_array c1, c2; /* the request's output arrays */
+    double queue_ms;         /* submit -> admitted */
+    double latency_ms;       /* submit -> GPU work complete */
+} ftx_result;
+struct ftx_server_s;
+typedef struct ftx_server_s *ftx_server;
+ft_error ftx_server_create(ftx_server *server, const uint8_t *pk, size_t hbm_budget_bytes, int slots);
+/* FT_ERR_INSUFFICIENT_SPACE if the request alone exceeds the budget */
+ft_error ftx_server_submit(ftx_server server, const ftx_request *req, uint64_t *ticket);
+/* blocks until the request completes */
+ft_error ftx_server_wait(ftx_server server, uint64_t ticket, ftx_result *result);
+/* bytes of the budget in use and requests queued / running */
+ft_error ftx_server_stats(ftx_server server, size_t *bytes_in_use, size_t *queued, size_t *running);
+void ftx_server_free(ftx_server server);
+
 /* Launch-shape knobs, set by the autotuner (libftcrypto_gb300/autotune.py)
  * or by hand.  ftx_tune returns FT_ERR_BAD_SIZE for an unsupported value;
  * ftx_tune_get returns the current value (-1 for an unknown knob). */

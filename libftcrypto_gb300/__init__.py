@@ -12,6 +12,6 @@ The C library is the product; this package builds it (build.py), binds it
 """
 from .api import (AFFINE, EXTENDED, FOLDED, PACKED, TUNE_BATCH_ADD_PTS, TUNE_LADDER_BLOCK, Array,  # noqa: F401
                   Batch, FtError, check, device_memory, encrypt, encrypt_device, error_str, init,
-                  segmented_sum_csr, segmented_sum_csr_device, stream_handle, synchronize, tune, tune_get)
+                  Server, segmented_sum_csr, segmented_sum_csr_device, stream_handle, synchronize, tune, tune_get)
 from .build import LIB as LIB_PATH  # noqa: F401
 from .build import build  # noqa: F401

@@ -86,6 +86,28 @@ SIGNATURES = {
     "ftx_scan_noalloc": (I, [P, S, S, I, P]),
 }
 
+class Request(ctypes.Structure):
+    """ftx_request of include/ftcrypto_gb300.h"""
+    _fields_ = [("op", ctypes.c_int), ("n", ctypes.c_size_t), ("m", ctypes.c_void_p),
+                ("plaintext_bits", ctypes.c_uint), ("r", ctypes.c_void_p), ("k", ctypes.c_void_p),
+                ("offsets", ctypes.c_void_p), ("nseg", ctypes.c_size_t), ("c1", ctypes.c_void_p),
+                ("c2", ctypes.c_void_p)]
+
+
+class Result(ctypes.Structure):
+    """ftx_result of include/ftcrypto_gb300.h"""
+    _fields_ = [("err", ctypes.c_int), ("c1", ctypes.c_void_p), ("c2", ctypes.c_void_p),
+                ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+SIGNATURES.update({
+    "ftx_server_create": (I, [PP, P, S, I]),
+    "ftx_server_submit": (I, [P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "ftx_server_wait": (I, [P, ctypes.c_uint64, ctypes.POINTER(Result)]),
+    "ftx_server_stats": (I, [P, PS, PS, PS]),
+    "ftx_server_free": (None, [P]),
+})
+
 REFERENCE_SYMBOLS = [k for k in SIGNATURES if k.startswith("ft_")]
 
 _lib = None

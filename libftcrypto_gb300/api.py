@@ -356,3 +356,73 @@ def tune_get(knob: int) -> int:
 
 TUNE_LADDER_BLOCK = 1
 TUNE_BATCH_ADD_PTS = 2
+
+
+REQ_ENCRYPT, REQ_RERAND, REQ_SMUL, REQ_SEGSUM = 1, 2, 3, 4
+
+
+class Server:
+    """ftx_server: continuous-batching request loop (see ftcrypto_gb300.h).
+    Host buffers of a request are kept alive until its result is taken."""
+
+    def __init__(self, pk32, hbm_budget_bytes: int, slots: int = 8):
+        pk = _buf(pk32, np.uint8).reshape(32)
+        h = ctypes.c_void_p()
+        check(lib().ftx_server_create(ctypes.byref(h), _ptr(pk), int(hbm_budget_bytes), int(slots)))
+        self._h = h
+        self._live = {}
+
+    def _submit(self, req, keep, in_place):
+        t = ctypes.c_uint64()
+        check(lib().ftx_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        self._live[t.value] = (keep, in_place)
+        return t.value
+
+    def submit_encrypt(self, m, r, plaintext_bits: int = 64) -> int:
+        mm, rr = _buf(m, np.uint64), _buf(r, np.uint8, 32)
+        req = _lib.Request(op=REQ_ENCRYPT, n=mm.size, m=mm.ctypes.data, plaintext_bits=plaintext_bits,
+                           r=rr.ctypes.data)
+        return self._submit(req, (mm, rr), None)
+
+    def submit_rerand(self, c1: Array, c2: Array, r) -> int:
+        rr = _buf(r, np.uint8, 32)
+        req = _lib.Request(op=REQ_RERAND, n=len(c1), r=rr.ctypes.data, c1=c1.handle.value, c2=c2.handle.value)
+        return self._submit(req, (rr,), (c1, c2))
+
+    def submit_smul(self, c1: Array, c2: Array, k) -> int:
+        kk = _buf(k, np.uint8, 32)
+        req = _lib.Request(op=REQ_SMUL, n=len(c1), k=kk.ctypes.data, c1=c1.handle.value, c2=c2.handle.value)
+        return self._submit(req, (kk,), (c1, c2))
+
+    def submit_segsum(self, c1: Array, c2: Array, offsets) -> int:
+        off = _buf(offsets, np.int32)
+        req = _lib.Request(op=REQ_SEGSUM, n=len(c1), offsets=off.ctypes.data, nseg=off.size - 1,
+                           c1=c1.handle.value, c2=c2.handle.value)
+        return self._submit(req, (off, c1, c2), None)
+
+    def wait(self, ticket: int):
+        """(c1, c2, queue_ms, latency_ms); new arrays for ENCRYPT / SEGSUM."""
+        res = _lib.Result()
+        check(lib().ftx_server_wait(self._h, ticket, ctypes.byref(res)))
+        keep, in_place = self._live.pop(ticket)
+        check(res.err)
+        if in_place is not None:
+            c1, c2 = in_place
+        else:
+            c1, c2 = Array(ctypes.c_void_p(res.c1)), Array(ctypes.c_void_p(res.c2))
+        return c1, c2, res.queue_ms, res.latency_ms
+
+    def stats(self):
+        a, b, c = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        check(lib().ftx_server_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().ftx_server_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.ftx_server_free(self._h)
+            self._h = None

@@ -937,6 +937,37 @@ ft_error ftx_scale_small(ft_ge25519_array array, uint32_t k)
 
 } // extern "C"
 
+// ---------------------------------------------------------------- serving helpers
+
+namespace ft {
+
+cudaMemPool_t host_pool() { return g.pool; }
+
+// comb table of a public key for a server (cudaMalloc'd; the server frees it)
+ft_error ftx_server_pk_table(const uint8_t *pk, uint32_t **table)
+{
+    ft_ge25519_array q;
+    int64_t bad = -1;
+    ft_error err = ft_array_from_bytes_folded(&bad, &q, pk, 32);
+    if (err) return err;
+    if (bad >= 0) {
+        ft_array_free(q);
+        return FT_ERR_INVALID_POINT;
+    }
+    cudaError_t e = cudaMalloc((void **)table, 32 * 8 * 24 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = build_comb_table(*table, view_of(q), g.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
+    ft_array_free(q);
+    if (e != cudaSuccess) {
+        if (*table) cudaFree(*table);
+        *table = nullptr;
+        return map_err(e);
+    }
+    return FT_ERR_NO_ERROR;
+}
+
+} // namespace ft
+
 // ---------------------------------------------------------------- batches
 
 struct ftx_batch_s {

@@ -1,0 +1,380 @@
+// serve.cu — the serving form (ftx_server_*): a request loop with
+// continuous batching over device-resident ciphertext arrays.
+//
+// One worker thread per server.  Requests are queued by submit() (any
+// thread) and admitted strictly in arrival order as soon as one of the
+// server's CUDA streams ("slots") is free and the request's device memory
+// fits the HBM budget.  An admitted request's inputs are staged and its
+// kernels queued on its slot's stream, so requests in flight overlap on the
+// GPU; a host callback at the end of the stream marks completion, and the
+// worker then returns the request's temporary memory and budget.  The
+// arithmetic is the library's, launched on the slot stream, so a request's
+// result does not depend on what else runs.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "internal.h"
+#include "../../include/ftcrypto.h"
+#include "../../include/ftcrypto_gb300.h"
+
+namespace ft {
+cudaMemPool_t host_pool(); // ft_api.cu
+}
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Req {
+    ftx_request r;
+    uint64_t ticket = 0;
+    size_t bytes = 0;
+    Clock::time_point t_submit, t_admit, t_done;
+    ftx_result res{};
+    int slot = -1;
+    bool done = false;      // set by the stream callback
+    bool finished = false;  // result published
+    std::vector<void *> tmp;
+};
+
+struct Slot {
+    cudaStream_t st = nullptr;
+    cudaEvent_t lib_done = nullptr; // orders the slot after the library stream
+    Req *req = nullptr;
+};
+
+size_t request_bytes(const ftx_request &r)
+{
+    const size_t pts = FT_PLANES_BYTES_PER_POINT;
+    switch (r.op) {
+    case FTX_REQ_ENCRYPT: return 2 * r.n * pts + r.n * 40 + 4096;
+    case FTX_REQ_RERAND: return 2 * r.n * pts + r.n * 40 + 4096;
+    case FTX_REQ_SMUL: return r.n * 32 + 4096;
+    case FTX_REQ_SEGSUM: return 2 * r.nseg * pts + (r.nseg + 1) * 4 + 2 * ft::segsum_scratch_bytes(r.n) + 8192;
+    default: return 0;
+    }
+}
+
+} // namespace
+
+struct ftx_server_s {
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Req *> pending;
+    std::map<uint64_t, Req *> reqs;
+    std::vector<Slot> slots;
+    size_t budget = 0, in_use = 0, running = 0;
+    uint64_t next_ticket = 1;
+    bool stop = false;
+    uint32_t *pk_table = nullptr;
+    int device = 0;
+    std::thread worker;
+
+    ft_error dispatch(Req *q, Slot &sl);
+    void loop();
+};
+
+static void CUDART_CB on_stream_done(void *arg)
+{
+    auto *pair = (std::pair<ftx_server, Req *> *)arg;
+    ftx_server s = pair->first;
+    Req *q = pair->second;
+    delete pair;
+    std::lock_guard<std::mutex> lk(s->mu);
+    q->t_done = Clock::now();
+    q->done = true;
+    s->cv_work.notify_all();
+}
+
+static cudaError_t alloc_on(Req *q, void **p, size_t bytes, cudaStream_t st)
+{
+    *p = nullptr;
+    if (!bytes) return cudaSuccess;
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, ft::host_pool(), st);
+    if (e == cudaSuccess) q->tmp.push_back(*p);
+    return e;
+}
+
+static cudaError_t new_array(ft_ge25519_array *out, size_t n, cudaStream_t st)
+{
+    auto *a = (ft_ge25519_array_s *)std::malloc(sizeof(ft_ge25519_array_s));
+    if (!a) return cudaErrorMemoryAllocation;
+    a->n = a->cap = n;
+    a->planes = nullptr;
+    cudaError_t e = n ? cudaMallocFromPoolAsync((void **)&a->planes, n * FT_PLANES_BYTES_PER_POINT, ft::host_pool(), st)
+                      : cudaSuccess;
+    if (e != cudaSuccess) {
+        std::free(a);
+        return e;
+    }
+    *out = a;
+    return cudaSuccess;
+}
+
+// queue the request's copies and kernels on the slot's stream
+ft_error ftx_server_s::dispatch(Req *q, Slot &sl)
+{
+    const ftx_request &r = q->r;
+    cudaStream_t st = sl.st;
+    // arrays handed in may still be written by work queued on the library's
+    // stream (ft_* calls return before their kernels finish)
+    cudaError_t e = cudaEventRecord(sl.lib_done, (cudaStream_t)ftx_stream());
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, sl.lib_done, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return FT_ERR_INTERNAL_LIBRARY_ERROR;
+    }
+    auto enc = [&](ft_ge25519_array a, ft_ge25519_array b, const uint64_t *hm, unsigned bits) -> cudaError_t {
+        void *dr, *dm;
+        cudaError_t x = alloc_on(q, &dr, r.n * 32, st);
+        if (x == cudaSuccess) x = alloc_on(q, &dm, r.n * 8, st);
+        if (x == cudaSuccess) x = cudaMemcpyAsync(dr, r.r, r.n * 32, cudaMemcpyHostToDevice, st);
+        if (x == cudaSuccess)
+            x = hm ? cudaMemcpyAsync(dm, hm, r.n * 8, cudaMemcpyHostToDevice, st) : cudaMemsetAsync(dm, 0, r.n * 8, st);
+        if (x == cudaSuccess)
+            x = ft::encrypt(ft::view_of(a), ft::view_of(b), r.n, (const uint8_t *)dr, (const uint64_t *)dm,
+                            (int)((bits + 3) / 4) + 1, pk_table, st);
+        return x;
+    };
+    switch (r.op) {
+    case FTX_REQ_ENCRYPT: {
+        e = new_array(&q->res.c1, r.n, st);
+        if (e == cudaSuccess) e = new_array(&q->res.c2, r.n, st);
+        if (e == cudaSuccess) e = enc(q->res.c1, q->res.c2, r.m, r.plaintext_bits);
+        break;
+    }
+    case FTX_REQ_RERAND: {
+        ft_ge25519_array z1 = nullptr, z2 = nullptr;
+        e = new_array(&z1, r.n, st);
+        if (e == cudaSuccess) e = new_array(&z2, r.n, st);
+        if (e == cudaSuccess) e = enc(z1, z2, nullptr, 1);
+        if (e == cudaSuccess) e = ft::add(ft::view_of(r.c1), ft::view_of(z1), r.n, 0, st);
+        if (e == cudaSuccess) e = ft::add(ft::view_of(r.c2), ft::view_of(z2), r.n, 0, st);
+        for (ft_ge25519_array z : {z1, z2})
+            if (z) {
+                q->tmp.push_back(z->planes);
+                std::free(z);
+            }
+        q->res.c1 = r.c1;
+        q->res.c2 = r.c2;
+        break;
+    }
+    case FTX_REQ_SMUL: {
+        void *dk;
+        e = alloc_on(q, &dk, r.n * 32, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dk, r.k, r.n * 32, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = ft::smul_var(ft::view_of(r.c1), r.n, (const uint8_t *)dk, 1, st);
+        if (e == cudaSuccess) e = ft::smul_var(ft::view_of(r.c2), r.n, (const uint8_t *)dk, 1, st);
+        q->res.c1 = r.c1;
+        q->res.c2 = r.c2;
+        break;
+    }
+    case FTX_REQ_SEGSUM: {
+        void *doff, *s1, *s2;
+        e = new_array(&q->res.c1, r.nseg, st);
+        if (e == cudaSuccess) e = new_array(&q->res.c2, r.nseg, st);
+        if (e == cudaSuccess) e = alloc_on(q, &doff, (r.nseg + 1) * 4, st);
+        if (e == cudaSuccess) e = alloc_on(q, &s1, ft::segsum_scratch_bytes(r.n), st);
+        if (e == cudaSuccess) e = alloc_on(q, &s2, ft::segsum_scratch_bytes(r.n), st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(doff, r.offsets, (r.nseg + 1) * 4, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = ft::segsum(ft::view_of(q->res.c1), (const int32_t *)doff, r.nseg, ft::view_of(r.c1), r.n, nullptr, 0,
+                           s1, st);
+        if (e == cudaSuccess)
+            e = ft::segsum(ft::view_of(q->res.c2), (const int32_t *)doff, r.nseg, ft::view_of(r.c2), r.n, nullptr, 0,
+                           s2, st);
+        break;
+    }
+    default: return FT_ERR_BAD_SIZE;
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? FT_ERR_OUT_OF_MEMORY : FT_ERR_INTERNAL_LIBRARY_ERROR;
+    }
+    auto *arg = new std::pair<ftx_server, Req *>(this, q);
+    if (cudaLaunchHostFunc(st, on_stream_done, arg) != cudaSuccess) {
+        delete arg;
+        cudaGetLastError();
+        return FT_ERR_INTERNAL_LIBRARY_ERROR;
+    }
+    return FT_ERR_NO_ERROR;
+}
+
+void ftx_server_s::loop()
+{
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    while (true) {
+        // reclaim completed requests
+        for (Slot &sl : slots) {
+            Req *q = sl.req;
+            if (!q || !q->done) continue;
+            for (void *p : q->tmp) cudaFreeAsync(p, sl.st);
+            q->tmp.clear();
+            in_use -= q->bytes;
+            running--;
+            q->res.queue_ms = std::chrono::duration<double, std::milli>(q->t_admit - q->t_submit).count();
+            q->res.latency_ms = std::chrono::duration<double, std::milli>(q->t_done - q->t_submit).count();
+            q->finished = true;
+            sl.req = nullptr;
+            cv_done.notify_all();
+        }
+        // admit in arrival order while a slot is free and memory fits
+        while (!pending.empty()) {
+            Req *q = pending.front();
+            if (in_use + q->bytes > budget) break;
+            Slot *free_slot = nullptr;
+            for (Slot &sl : slots)
+                if (!sl.req) {
+                    free_slot = &sl;
+                    break;
+                }
+            if (!free_slot) break;
+            pending.pop_front();
+            q->t_admit = Clock::now();
+            q->slot = (int)(free_slot - slots.data());
+            in_use += q->bytes;
+            running++;
+            free_slot->req = q;
+            lk.unlock(); // callbacks and submitters never wait on CUDA calls
+            ft_error err = dispatch(q, *free_slot);
+            lk.lock();
+            if (err) { // finish q with the error; its memory is released in stream order
+                q->res.err = err;
+                if (q->r.op == FTX_REQ_ENCRYPT || q->r.op == FTX_REQ_SEGSUM) {
+                    for (ft_ge25519_array *a : {&q->res.c1, &q->res.c2})
+                        if (*a) {
+                            if ((*a)->planes) cudaFreeAsync((*a)->planes, free_slot->st);
+                            std::free(*a);
+                            *a = nullptr;
+                        }
+                }
+                for (void *p : q->tmp) cudaFreeAsync(p, free_slot->st);
+                q->tmp.clear();
+                in_use -= q->bytes;
+                running--;
+                free_slot->req = nullptr;
+                q->t_done = Clock::now();
+                q->finished = true;
+                cv_done.notify_all();
+            }
+        }
+        if (stop && pending.empty() && running == 0) break;
+        cv_work.wait_for(lk, std::chrono::microseconds(200));
+    }
+}
+
+namespace ft {
+ft_error ftx_server_pk_table(const uint8_t *pk, uint32_t **table); // ft_api.cu
+}
+
+extern "C" {
+
+ft_error ftx_server_create(ftx_server *server, const uint8_t *pk, size_t hbm_budget_bytes, int slots)
+{
+    if (slots < 1 || slots > 64 || hbm_budget_bytes == 0) return FT_ERR_BAD_SIZE;
+    ft_error err = ft_crypto_init();
+    if (err) return err;
+    auto *s = new (std::nothrow) ftx_server_s();
+    if (!s) return FT_ERR_OUT_OF_MEMORY;
+    if ((err = ft::ftx_server_pk_table(pk, &s->pk_table))) {
+        delete s;
+        return err;
+    }
+    cudaGetDevice(&s->device);
+    s->budget = hbm_budget_bytes;
+    s->slots.resize(slots);
+    for (Slot &sl : s->slots) {
+        if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl.lib_done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            ftx_server_free(s);
+            return FT_ERR_INTERNAL_LIBRARY_ERROR;
+        }
+    }
+    s->worker = std::thread([s] { s->loop(); });
+    *server = s;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_server_submit(ftx_server s, const ftx_request *req, uint64_t *ticket)
+{
+    const ftx_request &r = *req;
+    if (r.op < FTX_REQ_ENCRYPT || r.op > FTX_REQ_SEGSUM) return FT_ERR_BAD_SIZE;
+    if (r.op == FTX_REQ_ENCRYPT && (r.plaintext_bits < 1 || r.plaintext_bits > 64)) return FT_ERR_BAD_SIZE;
+    if (r.op != FTX_REQ_ENCRYPT && (!r.c1 || !r.c2 || r.c1->n != r.n || r.c2->n != r.n)) return FT_ERR_SIZE_MISMATCH;
+    if (r.op == FTX_REQ_SEGSUM) {
+        if (r.n >= (size_t)INT32_MAX || r.offsets[0] != 0 || (size_t)r.offsets[r.nseg] != r.n) return FT_ERR_BAD_SIZE;
+        for (size_t i = 0; i < r.nseg; ++i)
+            if (r.offsets[i + 1] < r.offsets[i]) return FT_ERR_BAD_SIZE;
+    }
+    auto *q = new (std::nothrow) Req();
+    if (!q) return FT_ERR_OUT_OF_MEMORY;
+    q->r = r;
+    q->bytes = request_bytes(r);
+    if (q->bytes > s->budget) {
+        delete q;
+        return FT_ERR_INSUFFICIENT_SPACE;
+    }
+    q->t_submit = Clock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    q->ticket = s->next_ticket++;
+    s->reqs[q->ticket] = q;
+    s->pending.push_back(q);
+    *ticket = q->ticket;
+    s->cv_work.notify_all();
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_server_wait(ftx_server s, uint64_t ticket, ftx_result *result)
+{
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return FT_ERR_OUT_OF_BOUNDS;
+    Req *q = it->second;
+    s->cv_done.wait(lk, [q] { return q->finished; });
+    *result = q->res;
+    s->reqs.erase(it);
+    delete q;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_server_stats(ftx_server s, size_t *bytes_in_use, size_t *queued, size_t *running)
+{
+    std::lock_guard<std::mutex> lk(s->mu);
+    *bytes_in_use = s->in_use;
+    *queued = s->pending.size();
+    *running = s->running;
+    return FT_ERR_NO_ERROR;
+}
+
+void ftx_server_free(ftx_server s)
+{
+    if (!s) return;
+    if (s->worker.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stop = true;
+            s->cv_work.notify_all();
+        }
+        s->worker.join();
+    }
+    for (Slot &sl : s->slots) {
+        if (sl.st) {
+            cudaStreamSynchronize(sl.st);
+            cudaStreamDestroy(sl.st);
+        }
+        if (sl.lib_done) cudaEventDestroy(sl.lib_done);
+    }
+    for (auto &kv : s->reqs) delete kv.second;
+    if (s->pk_table) cudaFree(s->pk_table);
+    delete s;
+}
+
+} // extern "C"
