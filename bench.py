@@ -93,6 +93,13 @@ class Dist:
             self.pg.destroy_process_group()
 
 
+def aggregate(dist: Dist, ms_local: float, units_per_rank: float):
+    """Whole-job throughput of replicas: every rank processed units_per_rank
+    in ms_local; the job took the slowest rank's time."""
+    ms_max = dist.max(ms_local)
+    return ms_max, dist.ws * units_per_rank / (ms_max / 1e3)
+
+
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons while running."""
 
@@ -228,8 +235,7 @@ def headline(args, dist, ft, synth, torch, st):
     ms = t0.elapsed_time(t1)
     enc_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in marks)
     mul_ms = statistics.mean(b.elapsed_time(c) for _, b, c in marks) / 2
-    ms_max = dist.max(ms)
-    value = dist.ws * args.steps * N_CT * SMUL_PER_CT / (ms_max / 1e3)
+    ms_max, value = aggregate(dist, ms, args.steps * N_CT * SMUL_PER_CT)
 
     # bit-exact check of a sample of the final outputs against the oracle
     import oracle
@@ -483,7 +489,7 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=3):
             "launches": {"batched": 1, "plain": 2 * n_arrays}}
 
 
-def serving(ft, synth, torch, loads=(0.25, 0.5, 0.75, 1.0), n_req=40, budget=120 << 30, slots=8):
+def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slots=8):
     """Serving: requests of 1,024..4,194,304 ciphertexts (log-uniform), mix
     35% encrypt of {0,1}, 25% re-randomise, 20% variable-base scalar-mult
     mod L, 20% segmented sum of mean-32 segments; Poisson arrivals at a
@@ -527,9 +533,8 @@ def serving(ft, synth, torch, loads=(0.25, 0.5, 0.75, 1.0), n_req=40, budget=120
             return srv.submit_smul(*q["c"], k_pool[o:o + n])
         return srv.submit_segsum(*q["c"], q["off"])
 
-    def run_server(reqs, rate):
+    def run_server(reqs, arrivals):
         srv = ft.Server(pk, budget, slots)
-        arrivals = np.cumsum(g.exponential(1.0 / rate, len(reqs))) if rate else np.zeros(len(reqs))
         tickets, lat = [], []
         done = threading.Event()
 
@@ -554,8 +559,7 @@ def serving(ft, synth, torch, loads=(0.25, 0.5, 0.75, 1.0), n_req=40, budget=120
         srv.close()
         return np.array(lat), wall
 
-    def run_plain(reqs, rate):
-        arrivals = np.cumsum(g.exponential(1.0 / rate, len(reqs)))
+    def run_plain(reqs, arrivals):
         lat = []
         t0 = time.perf_counter()
         for q, a in zip(reqs, arrivals):
@@ -580,15 +584,16 @@ def serving(ft, synth, torch, loads=(0.25, 0.5, 0.75, 1.0), n_req=40, budget=120
 
     # capacity: every request submitted at once
     reqs = make_reqs(n_req)
-    _, wall = run_server(reqs, 0)
+    _, wall = run_server(reqs, np.zeros(n_req))
     capacity = n_req / wall
     out = {"capacity_req_per_s": capacity, "slots": slots, "budget_gb": budget / 2**30, "requests_per_level": n_req,
            "levels": []}
     for load in loads:
         reqs = make_reqs(n_req)
         ct = sum(q["n"] for q in reqs)
-        ls, ws = run_server(reqs, load * capacity)
-        lp, wp = run_plain(reqs, load * capacity)
+        arrivals = np.cumsum(g.exponential(1.0 / (load * capacity), n_req))  # one schedule for both
+        ls, ws = run_server(reqs, arrivals)
+        lp, wp = run_plain(reqs, arrivals)
         out["levels"].append({
             "offered_load": load, "offered_req_per_s": load * capacity,
             "server": {"p50_ms": float(np.percentile(ls, 50)), "p99_ms": float(np.percentile(ls, 99)),
@@ -672,6 +677,8 @@ def run_ours(args):
     ft.build()
     ft.init()
     st = torch.cuda.ExternalStream(ft.stream_handle())
+    from libftcrypto_gb300 import autotune
+    tuning = autotune.load_or_tune()
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     sms = torch.cuda.get_device_properties(dist.local).multi_processor_count
@@ -703,6 +710,7 @@ def run_ours(args):
         "gpu_launches": 3 * args.steps,
         "parity": {"sample_bit_exact_vs_oracle": h["parity_sample"], "sample": h["sample"]},
         "encrypt_ms": h["enc_ms"], "mul_ms_per_launch": h["mul_ms"],
+        "tuning": {k: v for k, v in tuning.items() if k != "timings_s"},
     }
     if dist.rank == 0:
         if not args.no_extras:

@@ -1,0 +1,111 @@
+"""Autotuner for the library's run-time launch-shape knobs (ftx_tune).
+
+Knobs and candidates:
+  FTX_TUNE_LADDER_BLOCK   block size of the variable-base ladder: 128, 192,
+                          224 threads (its shared-memory tables take 1 KB per
+                          thread, so this sets how many warps an SM holds)
+  FTX_TUNE_BATCH_ADD_PTS  points per thread of an ADD item of the batched
+                          form: 1, 2, 4, 8, 16 (item granularity against
+                          queue overhead)
+The window width of the ladder is not a knob: the reference's 4-bit signed
+window is kept because it fixes the sequence of group operations, which is
+what makes results agree with the reference on every input.
+
+Each candidate is timed on the device (best of three, synchronised wall
+clock) and the fastest is applied.  Results are cached per GPU model in
+$FT_TUNE_CACHE (default ~/.cache/libftcrypto_gb300/tune.json).
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+
+import numpy as np
+
+from . import api, synth
+
+CANDIDATES = {
+    api.TUNE_LADDER_BLOCK: (128, 192, 224),
+    api.TUNE_BATCH_ADD_PTS: (1, 2, 4, 8, 16),
+}
+NAMES = {api.TUNE_LADDER_BLOCK: "ladder_block", api.TUNE_BATCH_ADD_PTS: "batch_add_pts"}
+
+
+def cache_path() -> str:
+    return os.environ.get("FT_TUNE_CACHE", os.path.expanduser("~/.cache/libftcrypto_gb300/tune.json"))
+
+
+def _best_of(fn, reps=3):
+    best = float("inf")
+    for _ in range(reps):
+        api.synchronize()
+        t = time.perf_counter()
+        fn()
+        api.synchronize()
+        best = min(best, time.perf_counter() - t)
+    return best
+
+
+def device_key() -> str:
+    free, total = api.device_memory()
+    return f"sm103-{total >> 30}GiB"
+
+
+def tune(n_points: int = 1 << 18, seed: int = 7) -> dict:
+    """Time every candidate and apply the fastest; returns {knob: value}."""
+    g = synth.rng(seed)
+    sc = synth.scalars_mod_L(g, n_points)
+    base = api.Array.from_scalars(sc)
+    work = base.get_range(0, n_points, 1)
+    timings = {}
+    best = {}
+    for v in CANDIDATES[api.TUNE_LADDER_BLOCK]:
+        api.tune(api.TUNE_LADDER_BLOCK, v)
+        timings[f"ladder_block={v}"] = _best_of(lambda: work.mul(sc))
+    best[api.TUNE_LADDER_BLOCK] = min(CANDIDATES[api.TUNE_LADDER_BLOCK],
+                                      key=lambda v: timings[f"ladder_block={v}"])
+    api.tune(api.TUNE_LADDER_BLOCK, best[api.TUNE_LADDER_BLOCK])
+    # an uneven add-only batch: lengths log-uniform in [1, 65536]
+    lens = np.clip(np.floor(np.exp(g.uniform(0, np.log(65536), 256))), 1, 65536).astype(int)
+    pairs = [(base.get_range(0, min(n, n_points), 1), base.get_range(0, min(n, n_points), 1)) for n in lens]
+    for v in CANDIDATES[api.TUNE_BATCH_ADD_PTS]:
+        api.tune(api.TUNE_BATCH_ADD_PTS, v)
+        b = api.Batch()
+        for x, y in pairs:
+            b.add(x, y)
+        b.run()
+        timings[f"batch_add_pts={v}"] = _best_of(b.run)
+        b.free()
+    best[api.TUNE_BATCH_ADD_PTS] = min(CANDIDATES[api.TUNE_BATCH_ADD_PTS],
+                                       key=lambda v: timings[f"batch_add_pts={v}"])
+    api.tune(api.TUNE_BATCH_ADD_PTS, best[api.TUNE_BATCH_ADD_PTS])
+    result = {NAMES[k]: v for k, v in best.items()}
+    result["timings_s"] = timings
+    return result
+
+
+def load_or_tune(force: bool = False) -> dict:
+    """Apply the cached choice for this GPU model, tuning first if needed."""
+    path = cache_path()
+    key = device_key()
+    cache = {}
+    if os.path.exists(path):
+        try:
+            with open(path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+    if force or key not in cache:
+        cache[key] = tune()
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            with open(path, "w") as f:
+                json.dump(cache, f, indent=1)
+        except OSError:
+            pass
+    entry = cache[key]
+    for knob, name in NAMES.items():
+        if name in entry:
+            api.tune(knob, entry[name])
+    return entry
