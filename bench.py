@@ -45,9 +45,16 @@ METRIC = "EC scalar-mults/s & ciphertext adds/s on 1 GB300 (bit-exact); served p
 UNIT = "EC scalar-mults/s"
 N_CT = 1 << 20
 SMUL_PER_CT = 4
-FIELD_MULS_SMUL = 2340          # CT variable-base ladder, sodium_ge.cu:650-731
-PRODUCTS_PER_FIELD_MUL = 64     # 8 x 8 32-bit limb products
-W_ALG_SMUL = FIELD_MULS_SMUL * PRODUCTS_PER_FIELD_MUL
+# Algorithmic work in 32x32->64-bit products (the unit of the IMAD.WIDE peak):
+# a field multiplication is 64 limb products plus 9 for the fold by 38, a
+# squaring 36 + 9.  The CT variable-base ladder (sodium_ge.cu:650-731) does
+# 1,316 multiplications and 1,024 squarings: 48 M + 16 S for the table,
+# 63 x (20 M + 16 S) for the windows, 8 M for the last add.
+PRODUCTS_MUL = 64 + 9
+PRODUCTS_SQ = 36 + 9
+LADDER_MULS, LADDER_SQS = 1316, 1024
+W_ALG_SMUL = LADDER_MULS * PRODUCTS_MUL + LADDER_SQS * PRODUCTS_SQ  # 142,148
+W_ALG_PTADD = 9 * PRODUCTS_MUL  # extended + extended: to_cached, add, to_p3
 B_PT = 128                      # algorithmic bytes of one extended point
 SEED = 20240531
 
@@ -353,7 +360,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     ok = decrypt_matches(ft, s1, s2, sk[0], ma + mb)
     ms = timed(ev, lambda: (a1.add(b1), a2.add(b2)), 9, flush)
     out["ct_add_65536"] = {"ct_adds_per_s": n1 / (ms * 1e-3), "ms": ms, "decrypt_check": ok, "l2": "flushed",
-                           **roof(2 * n1 * 3 * B_PT, 2 * n1 * 9 * 64, ms, hbm_peak, imad)}
+                           **roof(2 * n1 * 3 * B_PT, 2 * n1 * W_ALG_PTADD, ms, hbm_peak, imad)}
 
     # full sum of 16,777,216 ciphertexts
     n3 = 1 << 24
@@ -365,7 +372,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     ok = decrypt_matches(ft, r1, r2, sk[0], [int(m3.sum())])
     ms = timed(ev, lambda: (c1.reduce_into(r1, 0), c2.reduce_into(r2, 0)), 3)
     out["reduce_16M_ct"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok,
-                            **roof(2 * n3 * B_PT, 2 * n3 * 9 * 64, ms, hbm_peak, imad)}
+                            **roof(2 * n3 * B_PT, 2 * n3 * W_ALG_PTADD, ms, hbm_peak, imad)}
 
     # segmented sum of the same 16,777,216 into 1,048,576 CSR segments
     nseg = 1 << 20
@@ -381,7 +388,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
                             ft.segmented_sum_csr_device(o2, d_off.data_ptr(), nseg, c2)), 3)
     seg_bytes = 2 * (n3 * B_PT + nseg * B_PT) + (nseg + 1) * 4
     out["segsum_16M_ct_1M_seg"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok,
-                                   **roof(seg_bytes, 2 * (n3 - nseg) * 9 * 64, ms, hbm_peak, imad)}
+                                   **roof(seg_bytes, 2 * (n3 - nseg) * W_ALG_PTADD, ms, hbm_peak, imad)}
     del c1, c2, o1, o2
 
     # inclusive scan of 4,194,304 ciphertexts
@@ -395,7 +402,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     ok = decrypt_matches(ft, t1.get_subset(idx), t2.get_subset(idx), sk[0], np.cumsum(m4)[idx])
     ms = timed(ev, lambda: (t1.scan(), t2.scan()), 3)
     out["scan_4M_ct"] = {"ct_per_s": n4 / (ms * 1e-3), "ms": ms, "decrypt_check_sample": ok,
-                         **roof(2 * n4 * 2 * B_PT, 2 * n4 * 9 * 64, ms, hbm_peak, imad)}
+                         **roof(2 * n4 * 2 * B_PT, 2 * n4 * W_ALG_PTADD, ms, hbm_peak, imad)}
     del c1, c2, t1, t2
     out["batched_uneven_4096"] = uneven_batch(ft, synth, torch, st)
     out["serving"] = serving(ft, synth, torch)
@@ -686,7 +693,9 @@ def run_ours(args):
     h = headline(args, dist, ft, synth, torch, st)
     e = e2e(args, dist, ft, torch, h.pop("state"))
     achieved = W_ALG_SMUL * N_CT / (h["mul_ms"] * 1e-3)
-    tr = profile_traffic().get("k_smul_var")
+    # the ladder kernel the tuned block size selects (> 256: tables half in TMEM)
+    kern = "k_smul_var_tm" if ft.tune_get(ft.TUNE_LADDER_BLOCK) > 256 else "k_smul_var"
+    tr = profile_traffic().get(kern)
     traffic = None
     if tr:
         traffic = tr["dram_bytes_per_point"] * N_CT
@@ -699,7 +708,7 @@ def run_ours(args):
                                "ciphertexts (4 EC scalar-mults per ciphertext)",
                    "n_ct": N_CT, "smul_per_ct": SMUL_PER_CT, "plaintext_bits": 8,
                    "l2": "no flush: working set 328 MB > 129 MB L2", "parallelism": f"replicas x{dist.ws}"},
-        "roofline": {"kernel": "k_smul_var (CT variable-base ladder)", "bound": "int",
+        "roofline": {"kernel": f"{kern} (CT variable-base ladder)", "bound": "int",
                      "achieved": achieved / 1e12, "peak": (imad or 0) / 1e12,
                      "unit": "T 32x32->64 mul-adds/s", "frac": (achieved / imad) if imad else None,
                      "traffic": traffic, "peak_source": "measured IMAD.WIDE probe (libftbench.so)",

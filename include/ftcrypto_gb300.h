@@ -17,6 +17,11 @@ extern "C" {
  * ft_neg, ft_index). */
 ft_error ftx_last_error(void);
 
+/* The CUDA runtime error (a cudaError_t value) behind the most recent
+ * FT_ERR_INTERNAL_LIBRARY_ERROR or FT_ERR_OUT_OF_MEMORY, 0 if none; a
+ * diagnostic only. */
+int ftx_last_cuda_error(void);
+
 /* The library's CUDA stream (a cudaStream_t) on which every call runs. */
 void *ftx_stream(void);
 
@@ -145,7 +150,8 @@ void ftx_server_free(ftx_server server);
 /* Launch-shape knobs, set by the autotuner (libftcrypto_gb300/autotune.py)
  * or by hand.  ftx_tune returns FT_ERR_BAD_SIZE for an unsupported value;
  * ftx_tune_get returns the current value (-1 for an unknown knob). */
-#define FTX_TUNE_LADDER_BLOCK 1  /* variable-base ladder block size: 128, 192 or 224 */
+#define FTX_TUNE_LADDER_BLOCK 1  /* variable-base ladder block size: 128, 192, 224 (tables in shared
+                                    memory) or 384, 448 (tables half in tensor memory) */
 #define FTX_TUNE_BATCH_ADD_PTS 2 /* batched form: points per thread of an ADD item (1..64) */
 ft_error ftx_tune(int knob, int value);
 int ftx_tune_get(int knob);

@@ -62,6 +62,7 @@ SIGNATURES = {
     "ft_array_reduce": (I, [P]),
     # extensions (ftcrypto_gb300.h)
     "ftx_last_error": (I, []),
+    "ftx_last_cuda_error": (I, []),
     "ftx_stream": (P, []),
     "ftx_synchronize": (I, []),
     "ftx_array_device_view": (I, [P, PP, PS]),

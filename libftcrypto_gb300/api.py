@@ -25,7 +25,10 @@ PACKED = 128
 class FtError(RuntimeError):
     def __init__(self, code: int):
         self.code = int(code)
-        super().__init__(f"ft_error {self.code}: {error_str(self.code)}")
+        msg = f"ft_error {self.code}: {error_str(self.code)}"
+        if self.code in (1, 9):  # out of memory, internal: name the CUDA error behind it
+            msg += f" (cudaError {lib().ftx_last_cuda_error()})"
+        super().__init__(msg)
 
 
 def lib():

@@ -2,8 +2,10 @@
 
 Knobs and candidates:
   FTX_TUNE_LADDER_BLOCK   block size of the variable-base ladder: 128, 192,
-                          224 threads (its shared-memory tables take 1 KB per
-                          thread, so this sets how many warps an SM holds)
+                          224 threads with the 1 KB per-thread tables in
+                          shared memory, or 384, 448 with half of each table
+                          in tensor memory (this sets how many warps an SM
+                          holds, against registers per thread)
   FTX_TUNE_BATCH_ADD_PTS  points per thread of an ADD item of the batched
                           form: 1, 2, 4, 8, 16 (item granularity against
                           queue overhead)
@@ -26,7 +28,7 @@ import numpy as np
 from . import api, synth
 
 CANDIDATES = {
-    api.TUNE_LADDER_BLOCK: (128, 192, 224),
+    api.TUNE_LADDER_BLOCK: (128, 192, 224, 384, 448),
     api.TUNE_BATCH_ADD_PTS: (1, 2, 4, 8, 16),
 }
 NAMES = {api.TUNE_LADDER_BLOCK: "ladder_block", api.TUNE_BATCH_ADD_PTS: "batch_add_pts"}

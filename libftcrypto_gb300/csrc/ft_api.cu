@@ -7,6 +7,7 @@
 // host data synchronise that stream.  CUDA failures become FT_ERR_* codes;
 // nothing here exits the process.
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -38,8 +39,11 @@ struct Ctx {
 Ctx g;
 std::mutex g_init_mu;
 
+std::atomic<int> g_last_cuda{0};
+
 ft_error map_err(cudaError_t e)
 {
+    g_last_cuda.store((int)e);
     cudaGetLastError();
     return e == cudaErrorMemoryAllocation ? FT_ERR_OUT_OF_MEMORY : FT_ERR_INTERNAL_LIBRARY_ERROR;
 }
@@ -759,6 +763,8 @@ ft_error ft_array_reduce(ft_ge25519_array array)
 // ---------------------------------------------------------------- extensions
 
 ft_error ftx_last_error(void) { return g.last_void; }
+
+int ftx_last_cuda_error(void) { return g_last_cuda.load(); }
 
 void *ftx_stream(void)
 {

@@ -66,6 +66,8 @@ cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *d_r, const uint64
 cudaError_t ladder_launch_128(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
 cudaError_t ladder_launch_192(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
 cudaError_t ladder_launch_224(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
+cudaError_t ladder_launch_384(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
+cudaError_t ladder_launch_448(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
 int ladder_block();
 int set_ladder_block(int nt);
 

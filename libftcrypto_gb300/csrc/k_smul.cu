@@ -186,13 +186,13 @@ __global__ void __launch_bounds__(256) k_comb_table(uint4 *out, const uint4 *q, 
 
 // ------------------------------------------------------------ launchers
 
-static int g_ladder_nt = 224;
+static int g_ladder_nt = 384; // tables half in TMEM: the fastest on GB300
 
 int ladder_block() { return g_ladder_nt; }
 
 int set_ladder_block(int nt)
 {
-    if (nt != 128 && nt != 192 && nt != 224) return -1;
+    if (nt != 128 && nt != 192 && nt != 224 && nt != 384 && nt != 448) return -1;
     g_ladder_nt = nt;
     return 0;
 }
@@ -204,7 +204,10 @@ cudaError_t smul_var(View v, size_t n, const uint8_t *sc, int sc_step, cudaStrea
     switch (g_ladder_nt) {
     case 128: return ladder_launch_128(v.p, v.s, n, s4, sc_step, st);
     case 192: return ladder_launch_192(v.p, v.s, n, s4, sc_step, st);
-    default: return ladder_launch_224(v.p, v.s, n, s4, sc_step, st);
+    case 384: return ladder_launch_384(v.p, v.s, n, s4, sc_step, st);
+    case 448: return ladder_launch_448(v.p, v.s, n, s4, sc_step, st);
+    case 224: return ladder_launch_224(v.p, v.s, n, s4, sc_step, st);
+    default: return ladder_launch_384(v.p, v.s, n, s4, sc_step, st);
     }
 }
 

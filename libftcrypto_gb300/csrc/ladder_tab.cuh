@@ -1,0 +1,121 @@
+// ladder_tab.cuh — per-thread tables of the variable-base ladder: (k+1)*P in
+// cached form for k < 8, 1 KB per thread.
+//   SmemTab<NT>    all entries in shared memory, [entry][16-byte word][thread]
+//                  with stride NT: a warp's access to one word of one entry
+//                  is 512 contiguous bytes (conflict-free).
+//   HybridTab<NT>  entries 0-3 in shared memory (same layout), 4-7 in the
+//                  thread's tensor-memory lane (tmem.cuh).
+// Both satisfy the Tab interface of smul.cuh.  This header holds no kernel,
+// so the host test harness compiles it against emulated shared and tensor
+// memory.
+#pragma once
+#include "smul.cuh"
+#include "u4.cuh"
+#ifndef FT_HOST_EMULATION
+#include "tmem.cuh"
+#define FT_TAB_FN __device__ __forceinline__
+#else
+#define FT_TAB_FN inline
+#endif
+
+namespace ft {
+
+template <int NT>
+struct SmemTab {
+    uint4 *b; // &smem[threadIdx.x]
+    FT_TAB_FN void put(int k, const ge_cached &c) const
+    {
+        uint4 *q = b + (size_t)k * 8 * NT;
+        q[0 * NT] = u4_lo(c.YplusX);
+        q[1 * NT] = u4_hi(c.YplusX);
+        q[2 * NT] = u4_lo(c.YminusX);
+        q[3 * NT] = u4_hi(c.YminusX);
+        q[4 * NT] = u4_lo(c.Z);
+        q[5 * NT] = u4_hi(c.Z);
+        q[6 * NT] = u4_lo(c.T2d);
+        q[7 * NT] = u4_hi(c.T2d);
+    }
+    // coordinate j of entry k: 0 YplusX, 1 YminusX, 2 Z, 3 T2d
+    FT_TAB_FN void get_fe(int k, int j, fe &f) const
+    {
+        const uint4 *q = b + (size_t)(k * 8 + 2 * j) * NT;
+        fe_from_u4(f, q[0], q[NT]);
+    }
+    FT_TAB_FN void select_fe(fe &f, int j, uint32_t babs, bool one) const { tab_select_fe(f, *this, j, babs, one); }
+    FT_TAB_FN void get(int k, ge_cached &c) const
+    {
+        const uint4 *q = b + (size_t)k * 8 * NT;
+        fe_from_u4(c.YplusX, q[0 * NT], q[1 * NT]);
+        fe_from_u4(c.YminusX, q[2 * NT], q[3 * NT]);
+        fe_from_u4(c.Z, q[4 * NT], q[5 * NT]);
+        fe_from_u4(c.T2d, q[6 * NT], q[7 * NT]);
+    }
+};
+
+// Entries 0-3 in shared memory ([entry][word][thread], stride NT), entries
+// 4-7 in TMEM at columns col + 32 j + 8 (k - 4) of the thread's lane: the
+// four entries' coordinate j are 32 consecutive columns, read by one load.
+template <int NT>
+struct HybridTab {
+    uint4 *b;     // &smem[threadIdx.x]
+    uint32_t col; // TMEM address of this warp's lane quarter and column slice
+    FT_TAB_FN void put(int k, const ge_cached &c) const
+    {
+        if (k < 4) {
+            uint4 *q = b + (size_t)k * 8 * NT;
+            q[0 * NT] = u4_lo(c.YplusX);
+            q[1 * NT] = u4_hi(c.YplusX);
+            q[2 * NT] = u4_lo(c.YminusX);
+            q[3 * NT] = u4_hi(c.YminusX);
+            q[4 * NT] = u4_lo(c.Z);
+            q[5 * NT] = u4_hi(c.Z);
+            q[6 * NT] = u4_lo(c.T2d);
+            q[7 * NT] = u4_hi(c.T2d);
+        } else {
+            const uint32_t a = col + 8u * (uint32_t)(k - 4);
+            tmem_st8(a + 0, c.YplusX.v);
+            tmem_st8(a + 32, c.YminusX.v);
+            tmem_st8(a + 64, c.Z.v);
+            tmem_st8(a + 96, c.T2d.v);
+        }
+    }
+    FT_TAB_FN void get(int k, ge_cached &c) const
+    {
+        if (k < 4) {
+            const uint4 *q = b + (size_t)k * 8 * NT;
+            fe_from_u4(c.YplusX, q[0 * NT], q[1 * NT]);
+            fe_from_u4(c.YminusX, q[2 * NT], q[3 * NT]);
+            fe_from_u4(c.Z, q[4 * NT], q[5 * NT]);
+            fe_from_u4(c.T2d, q[6 * NT], q[7 * NT]);
+        } else {
+            tmem_wait_st();
+            const uint32_t a = col + 8u * (uint32_t)(k - 4);
+            tmem_ld8(a + 0, c.YplusX.v);
+            tmem_ld8(a + 32, c.YminusX.v);
+            tmem_ld8(a + 64, c.Z.v);
+            tmem_ld8(a + 96, c.T2d.v);
+        }
+    }
+    FT_TAB_FN void select_fe(fe &f, int j, uint32_t babs, bool one) const
+    {
+        if (one) fe_1(f);
+        else fe_0(f);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint4 *q = b + (size_t)(k * 8 + 2 * j) * NT;
+            fe e;
+            fe_from_u4(e, q[0], q[NT]);
+            fe_cmov(f, e, ct_eq_mask(babs, (uint32_t)(k + 1)));
+        }
+        uint32_t r[32];
+        tmem_ld32(col + 32u * (uint32_t)j, r);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t m = ct_eq_mask(babs, (uint32_t)(k + 5));
+#pragma unroll
+            for (int w = 0; w < 8; ++w) f.v[w] ^= (f.v[w] ^ r[8 * k + w]) & m;
+        }
+    }
+};
+
+} // namespace ft

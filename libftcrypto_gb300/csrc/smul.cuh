@@ -11,43 +11,106 @@
 #pragma once
 #include "ge.cuh"
 
-// Tab: put(k, const ge_cached&), get(k, ge_cached&) for k in [0, 8)
+// Tab: put(k, const ge_cached&), get(k, ge_cached&) for k in [0, 8) and
+// select_fe(f, j, babs, one): coordinate j (0 YplusX, 1 YminusX, 2 Z, 3 T2d)
+// of entry babs - 1 in constant time, the identity's for babs = 0.
+//
+// Every entry is the reference's value: 2P, 4P, 6P, 8P are doublings of P,
+// 2P, 3P, 4P and 3P, 5P, 7P are P + 2P, P + 4P, P + 6P, as in the
+// reference.  Only the evaluation order differs: the odd multiples read the
+// cached even multiple back from the table, so at most two projective
+// points are live at once (the register peak of the kernel).
 template <class Tab>
 FT_DEV void smul_build_table(Tab &tab, const ge_p3 &p)
 {
     ge_cached c;
     ge_p1p1 t;
-    ge_p3 p2, p3, p4, q;
+    ge_p3 q, u;
     ge_p3_to_cached(c, p);
     tab.put(0, c); // 1P
     ge_p3_dbl(t, p);
-    ge_p1p1_to_p3(p2, t);
-    ge_p3_to_cached(c, p2);
-    tab.put(1, c); // 2P = 2*P
+    ge_p1p1_to_p3(q, t); // 2P
+    ge_p3_to_cached(c, q);
+    tab.put(1, c);
+    ge_p3_dbl(t, q);
+    ge_p1p1_to_p3(q, t); // 4P = 2*2P
+    ge_p3_to_cached(c, q);
+    tab.put(3, c);
+    ge_p3_dbl(t, q);
+    ge_p1p1_to_p3(u, t); // 8P = 2*4P
+    ge_p3_to_cached(c, u);
+    tab.put(7, c);
+    tab.get(3, c);
     ge_add(t, p, c);
-    ge_p1p1_to_p3(p3, t);
-    ge_p3_to_cached(c, p3);
-    tab.put(2, c); // 3P = P + 2P
-    ge_p3_dbl(t, p2);
-    ge_p1p1_to_p3(p4, t);
-    ge_p3_to_cached(c, p4);
-    tab.put(3, c); // 4P = 2*2P
+    ge_p1p1_to_p3(u, t); // 5P = P + 4P
+    ge_p3_to_cached(c, u);
+    tab.put(4, c);
+    tab.get(1, c);
     ge_add(t, p, c);
-    ge_p1p1_to_p3(q, t);
+    ge_p1p1_to_p3(q, t); // 3P = P + 2P
     ge_p3_to_cached(c, q);
-    tab.put(4, c); // 5P = P + 4P
-    ge_p3_dbl(t, p3);
-    ge_p1p1_to_p3(q, t);
-    ge_p3_to_cached(c, q);
-    tab.put(5, c); // 6P = 2*3P
+    tab.put(2, c);
+    ge_p3_dbl(t, q);
+    ge_p1p1_to_p3(u, t); // 6P = 2*3P
+    ge_p3_to_cached(c, u);
+    tab.put(5, c);
     ge_add(t, p, c);
-    ge_p1p1_to_p3(q, t);
-    ge_p3_to_cached(c, q);
-    tab.put(6, c); // 7P = P + 6P
-    ge_p3_dbl(t, p4);
-    ge_p1p1_to_p3(q, t);
-    ge_p3_to_cached(c, q);
-    tab.put(7, c); // 8P = 2*4P
+    ge_p1p1_to_p3(u, t); // 7P = P + 6P
+    ge_p3_to_cached(c, u);
+    tab.put(6, c);
+}
+
+// f = coordinate j of entry babs - 1 (the identity's coordinate, fe_1 or
+// fe_0 as `one` says, for babs = 0); all eight entries are read.  Used by
+// tables that hold every entry in one memory (Tab::get_fe).
+template <class Tab>
+FT_DEV void tab_select_fe(fe &f, const Tab &tab, int j, uint32_t babs, bool one)
+{
+    if (one) fe_1(f);
+    else fe_0(f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        fe e;
+        tab.get_fe(k, j, e);
+        fe_cmov(f, e, ct_eq_mask(babs, (uint32_t)(k + 1)));
+    }
+}
+
+// r = p + d * P for a signed digit d in [-8, 8], where tab holds (k+1)*P:
+// select_cached followed by ge_add (the same field operations on the same
+// values), with each coordinate of the entry selected just before the
+// multiplication that uses it, so that only two selected coordinates are
+// live at a time.
+template <class Tab>
+FT_DEV void ge_add_select(ge_p1p1 &r, const ge_p3 &p, const Tab &tab, int d)
+{
+    const uint32_t bneg = (uint32_t)d >> 31;
+    const uint32_t babs = (uint32_t)((d ^ -(int)bneg) + (int)bneg);
+    const uint32_t nm = 0u - bneg;
+    fe a, b, t0;
+    tab.select_fe(a, 0, babs, true);
+    tab.select_fe(b, 1, babs, true);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { // -P swaps YplusX and YminusX
+        uint32_t sw = (a.v[k] ^ b.v[k]) & nm;
+        a.v[k] ^= sw;
+        b.v[k] ^= sw;
+    }
+    fe_add(r.X, p.Y, p.X);
+    fe_sub(r.Y, p.Y, p.X);
+    fe_mul(r.Z, r.X, a);
+    fe_mul(r.Y, r.Y, b);
+    tab.select_fe(a, 3, babs, false);
+    fe_neg(b, a); // -P negates T2d
+    fe_cmov(a, b, nm);
+    fe_mul(r.T, a, p.T);
+    tab.select_fe(a, 2, babs, true);
+    fe_mul(r.X, p.Z, a);
+    fe_add(t0, r.X, r.X);
+    fe_sub(r.X, r.Z, r.Y);
+    fe_add(r.Y, r.Z, r.Y);
+    fe_add(r.Z, t0, r.T);
+    fe_sub(r.T, t0, r.T);
 }
 
 // h = a * P where tab holds (k+1)*P.  a is 8 little-endian words.
@@ -59,13 +122,10 @@ FT_DEV void smul_ladder(ge_p3 &h, const uint32_t a[8], const Tab &tab)
     ge_p3_0(h);
     ge_p1p1 r;
     ge_p2 s;
-    ge_cached t;
-    auto get = [&](int k, ge_cached &e) { tab.get(k, e); };
     int d = pop_top_nibble(b); // digit 63 carries no bias
 #pragma unroll 1
     for (int i = 63; i > 0; --i) {
-        select_cached(t, d, get);
-        ge_add(r, h, t);
+        ge_add_select(r, h, tab, d);
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
             ge_p1p1_to_p2(s, r);
@@ -74,8 +134,7 @@ FT_DEV void smul_ladder(ge_p3 &h, const uint32_t a[8], const Tab &tab)
         ge_p1p1_to_p3(h, r);
         d = pop_top_nibble(b) - 8;
     }
-    select_cached(t, d, get);
-    ge_add(r, h, t);
+    ge_add_select(r, h, tab, d);
     ge_p1p1_to_p3(h, r);
 }
 
@@ -90,13 +149,10 @@ FT_DEV void smul_ladder_u32(ge_p3 &h, uint32_t k, const Tab &tab)
     ge_p3_0(h);
     ge_p1p1 r;
     ge_p2 s;
-    ge_cached t;
-    auto get = [&](int j, ge_cached &e) { tab.get(j, e); };
     int d = (int)((b >> 32) & 15u) - 8;
 #pragma unroll 1
     for (int i = 8; i > 0; --i) {
-        select_cached(t, d, get);
-        ge_add(r, h, t);
+        ge_add_select(r, h, tab, d);
 #pragma unroll 1
         for (int j = 0; j < 4; ++j) {
             ge_p1p1_to_p2(s, r);
@@ -105,8 +161,7 @@ FT_DEV void smul_ladder_u32(ge_p3 &h, uint32_t k, const Tab &tab)
         ge_p1p1_to_p3(h, r);
         d = (int)((b >> (4 * (i - 1))) & 15u) - 8;
     }
-    select_cached(t, d, get);
-    ge_add(r, h, t);
+    ge_add_select(r, h, tab, d);
     ge_p1p1_to_p3(h, r);
 }
 

@@ -2,7 +2,7 @@
 // (fe.cuh, ge.cuh, smul.cuh) over the C stand-ins of ptx_emul.h, exported for
 // tests/test_devcode_host.py to compare with the oracle.  TEST HARNESS ONLY.
 #include <string.h>
-#include "../../libftcrypto_gb300/csrc/smul.cuh"
+#include "../../libftcrypto_gb300/csrc/ladder_tab.cuh"
 #define FT_TABLE_QUAL static const
 #define FT_WANT_BASE_COMB
 #include "../../libftcrypto_gb300/csrc/base_table.inc"
@@ -14,6 +14,11 @@ struct ArrTab {
     ge_cached e[8];
     void put(int k, const ge_cached &c) { e[k] = c; }
     void get(int k, ge_cached &c) const { c = e[k]; }
+    void get_fe(int k, int j, fe &f) const
+    {
+        f = j == 0 ? e[k].YplusX : j == 1 ? e[k].YminusX : j == 2 ? e[k].Z : e[k].T2d;
+    }
+    void select_fe(fe &f, int j, uint32_t babs, bool one) const { tab_select_fe(f, *this, j, babs, one); }
 };
 
 static void base_entry(int row, int k, ge_precomp &e)
@@ -24,6 +29,23 @@ static void base_entry(int row, int k, ge_precomp &e)
     memcpy(e.xy2d.v, w + 16, 32);
 }
 
+// the ladder over the tables of the tensor-memory kernel (block size nt,
+// 384 or 448): point i is run as thread i % nt of a block, with that
+// thread's shared-memory column and warp's tensor-memory slice
+template <int NT>
+static void mul_hybrid(uint8_t *pts, const uint8_t *scalars, size_t n)
+{
+    static uint4 smem[NT * 4 * 8];
+    for (size_t i = 0; i < n; ++i) {
+        const int t = (int)(i % NT), warp = t / 32;
+        ft::HybridTab<NT> tab{smem + t, tmem_warp_addr(0u, warp, 128u * (uint32_t)(warp >> 2)) + (uint32_t)(t % 32 << 16)};
+        ge_p3 p, h; uint32_t a[8];
+        ld(p, pts + 128 * i); memcpy(a, scalars + 32 * i, 32);
+        smul_build_table(tab, p);
+        smul_ladder(h, a, tab);
+        st(pts + 128 * i, h);
+    }
+}
 extern "C" {
 
 void hc_fe_mul(uint32_t *h, const uint32_t *a, const uint32_t *b)
@@ -56,6 +78,13 @@ void hc_mul(uint8_t *pts, const uint8_t *scalars, size_t n)
         smul_ladder(h, a, tab);
         st(pts + 128 * i, h);
     }
+}
+int hc_mul_hybrid(uint8_t *pts, const uint8_t *scalars, size_t n, int nt)
+{
+    if (nt == 384) mul_hybrid<384>(pts, scalars, n);
+    else if (nt == 448) mul_hybrid<448>(pts, scalars, n);
+    else return -1;
+    return 0;
 }
 void hc_mul_u32(uint8_t *pts, const uint32_t *k, size_t n)
 {

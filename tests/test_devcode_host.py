@@ -83,6 +83,22 @@ def test_group_and_smul(hc, orc):
     assert (e == orc.encode(om)).all()
 
 
+@pytest.mark.parametrize("nt", [384, 448])
+def test_hybrid_table_ladder(hc, orc, nt):
+    """The ladder over the tensor-memory kernel's tables (half in shared
+    memory, half in an emulated TMEM that aborts on an out-of-range column)
+    gives the oracle's coordinates for threads in every warp slot."""
+    g = synth.rng(nt)
+    n = nt + 40  # every thread of a block, then a second block's first warps
+    sc = synth.scalars_mod_L(g, n)
+    for i, x in enumerate([0, 1, synth.L - 1, 2**256 - 1, 2**255 + 12345]):
+        sc[i] = synth.int_to_scalar(x)
+    p = orc.from_scalars(np.ascontiguousarray(sc[::-1]), threads=8)
+    m = p.copy()
+    assert hc.hc_mul_hybrid(ptr(m), ptr(sc), n, nt) == 0
+    assert (m == orc.mul(p, sc, threads=8)).all()
+
+
 def test_decode_and_small_comb(hc, orc):
     g = synth.rng(4)
     good = orc.encode(orc.from_scalars(synth.scalars_mod_L(g, 20)))

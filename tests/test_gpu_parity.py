@@ -139,6 +139,28 @@ def test_add_sub_mul_vs_oracle(ft, orc, n):
     assert (M.to_bytes_folded() == orc.encode(om)).all()
 
 
+@pytest.mark.parametrize("block", [128, 192, 224, 384, 448])
+def test_ladder_block_sizes(ft, orc, block):
+    """Every ladder kernel (tables in shared memory, or half in tensor memory
+    for 384 and 448) gives the oracle's coordinates word for word, with
+    partial last blocks and edge scalars."""
+    g = synth.rng(40 + block)
+    before = ft.tune_get(ft.TUNE_LADDER_BLOCK)
+    ft.tune(ft.TUNE_LADDER_BLOCK, block)
+    try:
+        for n in (1, block - 1, block + 1, 3 * block + 37):
+            a = rand_points(orc, g, n)
+            k = synth.scalars_mod_L(g, n)
+            edge = [0, 1, synth.L - 1, 2**255 - 1, 2**256 - 1]
+            for j, v in enumerate(edge[:n]):
+                k[j] = synth.int_to_scalar(v)
+            M = upload(ft, a)
+            M.mul(k)
+            assert (M.to_packed() == orc.mul(a, k, threads=8)).all(), n
+    finally:
+        ft.tune(ft.TUNE_LADDER_BLOCK, before)
+
+
 def test_aliasing_and_size_mismatch(ft, orc):
     g = synth.rng(7)
     a = rand_points(orc, g, 33)
