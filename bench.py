@@ -45,16 +45,19 @@ METRIC = "EC scalar-mults/s & ciphertext adds/s on 1 GB300 (bit-exact); served p
 UNIT = "EC scalar-mults/s"
 N_CT = 1 << 20
 SMUL_PER_CT = 4
-# Algorithmic work in 32x32->64-bit products (the unit of the IMAD.WIDE peak):
-# a field multiplication is 64 limb products plus 9 for the fold by 38, a
-# squaring 36 + 9.  The CT variable-base ladder (sodium_ge.cu:650-731) does
-# 1,316 multiplications and 1,024 squarings: 48 M + 16 S for the table,
-# 63 x (20 M + 16 S) for the windows, 8 M for the last add.
-PRODUCTS_MUL = 64 + 9
-PRODUCTS_SQ = 36 + 9
-LADDER_MULS, LADDER_SQS = 1316, 1024
-W_ALG_SMUL = LADDER_MULS * PRODUCTS_MUL + LADDER_SQS * PRODUCTS_SQ  # 142,148
-W_ALG_PTADD = 9 * PRODUCTS_MUL  # extended + extended: to_cached, add, to_p3
+# Algorithmic work in 32x32->64-bit products (the unit of the IMAD.WIDE peak),
+# the survey's unit: every field multiplication or squaring counts as one
+# 8 x 8-word schoolbook, 64 products.  The CT variable-base ladder
+# (sodium_ge.cu:650-731) is 2,340 of them (1,316 M + 1,024 S: 48 M + 16 S
+# for the table, 63 x (20 M + 16 S) for the windows, 8 M for the last add);
+# a point addition is 9 M.
+PRODUCTS_PER_FIELD_OP = 64
+FIELD_OPS_SMUL = 2340
+W_ALG_SMUL = FIELD_OPS_SMUL * PRODUCTS_PER_FIELD_OP  # 149,760
+W_ALG_PTADD = 9 * PRODUCTS_PER_FIELD_OP
+# The exact count, beside it: 64 limb products per multiplication, 36 per
+# squaring, 9 more for the fold by 38 of either.
+W_EXACT_SMUL = 1316 * (64 + 9) + 1024 * (36 + 9)  # 142,148
 B_PT = 128                      # algorithmic bytes of one extended point
 SEED = 20240531
 
@@ -496,14 +499,18 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=3):
             "launches": {"batched": 1, "plain": 2 * n_arrays}}
 
 
+SMALL_REQ = 65536  # "small" requests in the serving report: at most this many ciphertexts
+
+
 def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slots=8):
     """Serving: requests of 1,024..4,194,304 ciphertexts (log-uniform), mix
     35% encrypt of {0,1}, 25% re-randomise, 20% variable-base scalar-mult
     mod L, 20% segmented sum of mean-32 segments; Poisson arrivals at a
     fraction of the measured capacity; 120 GB admission budget.  p50 / p99
-    latency (arrival -> GPU work complete) and throughput, for the server
-    (continuous batching over `slots` streams) and for the plain drop-in
-    called once per request on the same arrival schedule."""
+    latency (arrival -> GPU work complete), also over the small requests
+    (<= SMALL_REQ ciphertexts), and throughput, for the server (continuous
+    batching over `slots` streams, half of them express) and for the plain
+    drop-in called once per request on the same arrival schedule."""
     import threading
     g = synth.rng(SEED + 21)
     sk = synth.scalars_mod_L(g, 1)
@@ -601,12 +608,16 @@ def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slot
         arrivals = np.cumsum(g.exponential(1.0 / (load * capacity), n_req))  # one schedule for both
         ls, ws = run_server(reqs, arrivals)
         lp, wp = run_plain(reqs, arrivals)
-        out["levels"].append({
-            "offered_load": load, "offered_req_per_s": load * capacity,
-            "server": {"p50_ms": float(np.percentile(ls, 50)), "p99_ms": float(np.percentile(ls, 99)),
-                       "req_per_s": n_req / ws, "ct_per_s": ct / ws},
-            "plain_per_request": {"p50_ms": float(np.percentile(lp, 50)), "p99_ms": float(np.percentile(lp, 99)),
-                                  "req_per_s": n_req / wp, "ct_per_s": ct / wp}})
+        small = np.array([q["n"] <= SMALL_REQ for q in reqs])
+
+        def stats(lat, wall):
+            return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                    "small_p50_ms": float(np.percentile(lat[small], 50)) if small.any() else None,
+                    "small_p99_ms": float(np.percentile(lat[small], 99)) if small.any() else None,
+                    "req_per_s": n_req / wall, "ct_per_s": ct / wall}
+        out["levels"].append({"offered_load": load, "offered_req_per_s": load * capacity,
+                              "small_requests": int(small.sum()),
+                              "server": stats(ls, ws), "plain_per_request": stats(lp, wp)})
         del reqs
     return out
 
@@ -713,6 +724,8 @@ def run_ours(args):
                      "unit": "T 32x32->64 mul-adds/s", "frac": (achieved / imad) if imad else None,
                      "traffic": traffic, "peak_source": "measured IMAD.WIDE probe (libftbench.so)",
                      "algorithmic": f"{W_ALG_SMUL} products per scalar-mult x {N_CT} per launch",
+                     "exact_products_per_smul": W_EXACT_SMUL,
+                     "frac_exact": (W_EXACT_SMUL * N_CT / (h["mul_ms"] * 1e-3) / imad) if imad else None,
                      "launch_ms": h["mul_ms"], "hbm_peak_gbs": hbm, "hbm_peak_source": peak_kind},
         "e2e": e,
         "clocks": h["clocks"],

@@ -104,12 +104,15 @@ ft_error ftx_batch_info(ftx_batch batch, size_t *n_items, size_t *n_ops);
 void ftx_batch_free(ftx_batch batch);
 
 /* Serving form: a request loop with continuous batching.  A server owns a
- * public key, a budget of device memory and `slots` CUDA streams.  Requests
- * are queued by ftx_server_submit from any thread and admitted in arrival
- * order as soon as a slot is free and their device memory (outputs, staged
- * inputs, scratch) fits in the budget; admitted requests run concurrently,
- * so work of requests arriving while others are on the GPU overlaps with
- * theirs.  Ciphertexts stay on the device as handles: ENCRYPT and SEGSUM
+ * public key, a budget of device memory and `slots` CUDA streams, the later
+ * half of them at the device's highest stream priority (express slots).
+ * Requests are queued by ftx_server_submit from any thread and admitted as
+ * soon as a slot is free and their device memory (outputs, staged inputs,
+ * scratch) fits in the budget: in arrival order among large requests, and
+ * among small ones (work below a few milliseconds of GPU time), which use
+ * the express slots first and may overtake queued large requests.  Admitted
+ * requests run concurrently, so work of requests arriving while others are
+ * on the GPU overlaps with theirs.  Ciphertexts stay on the device as handles: ENCRYPT and SEGSUM
  * create new arrays (the caller frees them with ft_array_free), RERAND and
  * SMUL update the given arrays in place.  Host buffers named in a request
  * must stay valid until its result is returned; arrays of a request must not

@@ -2,18 +2,27 @@
 // continuous batching over device-resident ciphertext arrays.
 //
 // One worker thread per server.  Requests are queued by submit() (any
-// thread) and admitted strictly in arrival order as soon as one of the
-// server's CUDA streams ("slots") is free and the request's device memory
-// fits the HBM budget.  An admitted request's inputs are staged and its
-// kernels queued on its slot's stream, so requests in flight overlap on the
-// GPU; a host callback at the end of the stream marks completion, and the
-// worker then returns the request's temporary memory and budget.  The
-// arithmetic is the library's, launched on the slot stream, so a request's
-// result does not depend on what else runs.
+// thread) and admitted as soon as one of the server's CUDA streams ("slots")
+// is free and the request's device memory fits the HBM budget.  An admitted
+// request's inputs are staged and its kernels queued on its slot's stream,
+// so requests in flight overlap on the GPU; a host callback at the end of
+// the stream marks completion, and the worker then returns the request's
+// temporary memory and budget.  The arithmetic is the library's, launched on
+// the slot stream, so a request's result does not depend on what else runs.
+//
+// Express lane: the request mix spans four orders of magnitude of work, and
+// the block scheduler dispatches a kernel's blocks in launch order, so a
+// small request queued behind a large one waits for nearly all of it.  Half
+// of the slots (the later ones) are created at the device's highest stream
+// priority; requests whose estimated work is at most EXPRESS_COST ladder
+// points (a few milliseconds of GPU time) prefer those slots, and their
+// blocks are dispatched as soon as SMs free up.  Admission is FIFO within
+// each class; an express request may overtake queued bulk requests (the
+// requests of a server touch disjoint arrays, so order does not matter).
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
-#include <deque>
+#include <list>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -38,6 +47,7 @@ struct Req {
     Clock::time_point t_submit, t_admit, t_done;
     ftx_result res{};
     int slot = -1;
+    bool express = false;   // small enough for the high-priority slots
     bool done = false;      // set by the stream callback
     bool finished = false;  // result published
     std::vector<void *> tmp;
@@ -47,7 +57,23 @@ struct Slot {
     cudaStream_t st = nullptr;
     cudaEvent_t lib_done = nullptr; // orders the slot after the library stream
     Req *req = nullptr;
+    bool express = false;           // created at the highest stream priority
 };
+
+// estimated work in variable-base ladder points (the ladder is the unit:
+// one encryption costs ~0.65 of one, a point addition ~1/40)
+constexpr double EXPRESS_COST = 131072.0;
+
+double request_cost(const ftx_request &r)
+{
+    switch (r.op) {
+    case FTX_REQ_ENCRYPT: return 0.65 * (double)r.n;
+    case FTX_REQ_RERAND: return 0.7 * (double)r.n;
+    case FTX_REQ_SMUL: return 2.0 * (double)r.n;
+    case FTX_REQ_SEGSUM: return 0.06 * (double)r.n;
+    default: return 0.0;
+    }
+}
 
 size_t request_bytes(const ftx_request &r)
 {
@@ -66,7 +92,7 @@ size_t request_bytes(const ftx_request &r)
 struct ftx_server_s {
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<Req *> pending;
+    std::list<Req *> pending; // iterators stay valid while submitters append
     std::map<uint64_t, Req *> reqs;
     std::vector<Slot> slots;
     size_t budget = 0, in_use = 0, running = 0;
@@ -77,6 +103,8 @@ struct ftx_server_s {
     std::thread worker;
 
     ft_error dispatch(Req *q, Slot &sl);
+    Slot *free_slot(bool express);
+    void admit(std::unique_lock<std::mutex> &lk, Req *q, Slot *sl);
     void loop();
 };
 
@@ -206,6 +234,52 @@ ft_error ftx_server_s::dispatch(Req *q, Slot &sl)
     return FT_ERR_NO_ERROR;
 }
 
+// a free slot for a request of the class: express requests take an express
+// slot if one is free, else any; bulk requests only bulk slots
+Slot *ftx_server_s::free_slot(bool express)
+{
+    Slot *any = nullptr;
+    for (Slot &sl : slots) {
+        if (sl.req) continue;
+        if (sl.express == express) return &sl;
+        if (express && !any) any = &sl;
+    }
+    return any;
+}
+
+// start q on sl (called with the lock held; dispatch runs unlocked so that
+// callbacks and submitters never wait on CUDA calls)
+void ftx_server_s::admit(std::unique_lock<std::mutex> &lk, Req *q, Slot *sl)
+{
+    q->t_admit = Clock::now();
+    q->slot = (int)(sl - slots.data());
+    in_use += q->bytes;
+    running++;
+    sl->req = q;
+    lk.unlock();
+    ft_error err = dispatch(q, *sl);
+    lk.lock();
+    if (!err) return;
+    // finish q with the error; its memory is released in stream order
+    q->res.err = err;
+    if (q->r.op == FTX_REQ_ENCRYPT || q->r.op == FTX_REQ_SEGSUM) {
+        for (ft_ge25519_array *a : {&q->res.c1, &q->res.c2})
+            if (*a) {
+                if ((*a)->planes) cudaFreeAsync((*a)->planes, sl->st);
+                std::free(*a);
+                *a = nullptr;
+            }
+    }
+    for (void *p : q->tmp) cudaFreeAsync(p, sl->st);
+    q->tmp.clear();
+    in_use -= q->bytes;
+    running--;
+    sl->req = nullptr;
+    q->t_done = Clock::now();
+    q->finished = true;
+    cv_done.notify_all();
+}
+
 void ftx_server_s::loop()
 {
     cudaSetDevice(device);
@@ -225,45 +299,25 @@ void ftx_server_s::loop()
             sl.req = nullptr;
             cv_done.notify_all();
         }
-        // admit in arrival order while a slot is free and memory fits
-        while (!pending.empty()) {
-            Req *q = pending.front();
-            if (in_use + q->bytes > budget) break;
-            Slot *free_slot = nullptr;
-            for (Slot &sl : slots)
-                if (!sl.req) {
-                    free_slot = &sl;
-                    break;
-                }
-            if (!free_slot) break;
-            pending.pop_front();
-            q->t_admit = Clock::now();
-            q->slot = (int)(free_slot - slots.data());
-            in_use += q->bytes;
-            running++;
-            free_slot->req = q;
-            lk.unlock(); // callbacks and submitters never wait on CUDA calls
-            ft_error err = dispatch(q, *free_slot);
-            lk.lock();
-            if (err) { // finish q with the error; its memory is released in stream order
-                q->res.err = err;
-                if (q->r.op == FTX_REQ_ENCRYPT || q->r.op == FTX_REQ_SEGSUM) {
-                    for (ft_ge25519_array *a : {&q->res.c1, &q->res.c2})
-                        if (*a) {
-                            if ((*a)->planes) cudaFreeAsync((*a)->planes, free_slot->st);
-                            std::free(*a);
-                            *a = nullptr;
-                        }
-                }
-                for (void *p : q->tmp) cudaFreeAsync(p, free_slot->st);
-                q->tmp.clear();
-                in_use -= q->bytes;
-                running--;
-                free_slot->req = nullptr;
-                q->t_done = Clock::now();
-                q->finished = true;
-                cv_done.notify_all();
+        // admit in arrival order within each class while a slot is free and
+        // memory fits; a bulk request that cannot start holds the later bulk
+        // ones back, an express one the later express ones
+        bool bulk_open = true, express_open = true;
+        for (auto it = pending.begin(); it != pending.end() && (bulk_open || express_open);) {
+            Req *q = *it;
+            bool &open = q->express ? express_open : bulk_open;
+            if (!open) {
+                ++it;
+                continue;
             }
+            Slot *sl = in_use + q->bytes <= budget ? free_slot(q->express) : nullptr;
+            if (!sl) {
+                open = false;
+                ++it;
+                continue;
+            }
+            it = pending.erase(it);
+            admit(lk, q, sl);
         }
         if (stop && pending.empty() && running == 0) break;
         cv_work.wait_for(lk, std::chrono::microseconds(200));
@@ -290,8 +344,14 @@ ft_error ftx_server_create(ftx_server *server, const uint8_t *pk, size_t hbm_bud
     cudaGetDevice(&s->device);
     s->budget = hbm_budget_bytes;
     s->slots.resize(slots);
-    for (Slot &sl : s->slots) {
-        if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess ||
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    const int n_bulk = (slots + 1) / 2;
+    for (int i = 0; i < slots; ++i) {
+        Slot &sl = s->slots[i];
+        sl.express = i >= n_bulk;
+        if (cudaStreamCreateWithPriority(&sl.st, cudaStreamNonBlocking, sl.express ? prio_high : prio_low) !=
+                cudaSuccess ||
             cudaEventCreateWithFlags(&sl.lib_done, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();
             ftx_server_free(s);
@@ -318,6 +378,7 @@ ft_error ftx_server_submit(ftx_server s, const ftx_request *req, uint64_t *ticke
     if (!q) return FT_ERR_OUT_OF_MEMORY;
     q->r = r;
     q->bytes = request_bytes(r);
+    q->express = request_cost(r) <= EXPRESS_COST;
     if (q->bytes > s->budget) {
         delete q;
         return FT_ERR_INSUFFICIENT_SPACE;
