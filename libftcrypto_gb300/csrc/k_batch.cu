@@ -1,31 +1,56 @@
 // k_batch.cu — the batched form: one persistent kernel for thousands of
 // independent, uneven array operations, and the small-scalar ladder.
 //
-// k_batch: one block per SM (224 threads: the shared-memory ladder tables
-//   of the scale path fill the SM) loops pulling work items from an atomic
-//   counter until the list is exhausted.  Items are pre-sorted costliest
-//   first, so the tail of the run is short ones (longest-processing-time
-//   order).  Item kinds:
-//     ADD    dst[i] += src[i] for count points (count <= 224 x points/thread)
-//     SCALE  dst[i] = k * dst[i], count <= 224 points, one per thread,
+// k_batch: one block per SM (384 threads: the ladder tables of the scale
+//   path fill the SM's shared memory and half of its tensor memory, as in
+//   k_smul_var_tm) loops pulling work items from an atomic counter until the
+//   list is exhausted.  Items are pre-sorted costliest first, so the tail of
+//   the run is short ones (longest-processing-time order).  Item kinds:
+//     ADD    dst[i] += src[i] for count points (count <= 384 x points/thread)
+//     SCALE  dst[i] = k * dst[i], count <= 384 points, one per thread,
 //            constant time in k < 2^32 (smul_ladder_u32)
-//     SEG    dst[s] = sum of src[off[s] .. off[s+1]), count <= 224 segments,
+//     SEG    dst[s] = sum of src[off[s] .. off[s+1]), count <= 384 segments,
 //            one per thread (segments of the batched workload are short)
 //   The host side (ft_api.cu, ftx_batch_*) captures {counter reset, k_batch}
 //   in a CUDA graph and replays it.
 // k_scale_small: ftx_scale_small, the same small-scalar ladder over one array.
+//
+// Both kernels allocate all 512 TMEM columns from warp 0 at entry and free
+// them after a final barrier (tmem.cuh); their shared memory admits one
+// block per SM.  In a SCALE item the warps past the item's count skip it
+// (a warp-uniform test) and the lanes past it in the last warp run the
+// ladder on the identity and store nothing, so every warp executes the
+// warp-wide tcgen05 instructions converged.
 #include "internal.h"
 #include "ladder.cuh"
 
 namespace ft {
 
-static constexpr int BATCH_NT = 224;
+static constexpr int BATCH_NT = 384;
 
-__global__ void __launch_bounds__(BATCH_NT, 1) k_batch(const BatchItem *items, int nitems, int *counter)
+// k * (point i of p) for the lanes with live set, the identity for the rest
+FT_DEV void scale_small_lane(uint4 *p, size_t s, size_t i, bool live, uint32_t k, const HybridTab<BATCH_NT> &tab)
+{
+    ge_p3 P, h;
+    if (live) ld_p3(P, p, s, i);
+    else ge_p3_0(P);
+    __syncwarp();
+    smul_build_table(tab, P);
+    tmem_wait_st();
+    smul_ladder_u32(h, k, tab);
+    if (live) st_p3(p, s, i, h);
+}
+
+__global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
+    k_batch(const BatchItem *items, int nitems, int *counter)
 {
     extern __shared__ uint4 smem[];
     __shared__ int s_item;
-    const int tid = threadIdx.x;
+    __shared__ uint32_t s_taddr;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tmem_alloc(&s_taddr, 512u);
+    tmem_sync_threads();
+    const HybridTab<BATCH_NT> tab{smem + tid, tmem_warp_addr(s_taddr, warp, 128u * (uint32_t)(warp >> 2))};
     for (;;) {
         if (tid == 0) s_item = atomicAdd(counter, 1);
         __syncthreads();
@@ -43,14 +68,8 @@ __global__ void __launch_bounds__(BATCH_NT, 1) k_batch(const BatchItem *items, i
                 st_p3(w.dst, w.dst_s, e, x);
             }
         } else if (w.op == BATCH_SCALE) {
-            if ((uint32_t)tid < w.count) {
-                SmemTab<BATCH_NT> tab{smem + tid};
-                ge_p3 P, h;
-                ld_p3(P, w.dst, w.dst_s, tid);
-                smul_build_table(tab, P);
-                smul_ladder_u32(h, w.k, tab);
-                st_p3(w.dst, w.dst_s, tid, h);
-            }
+            if ((uint32_t)(warp * 32) < w.count) // warp-uniform
+                scale_small_lane(w.dst, w.dst_s, tid, (uint32_t)tid < w.count, w.k, tab);
         } else { // BATCH_SEG
 #pragma unroll 1
             for (uint32_t sg = tid; sg < w.count; sg += BATCH_NT) {
@@ -68,19 +87,24 @@ __global__ void __launch_bounds__(BATCH_NT, 1) k_batch(const BatchItem *items, i
             }
         }
     }
+    tmem_sync_threads();
+    if (warp == 0) tmem_free(s_taddr, 512u);
 }
 
-__global__ void __launch_bounds__(BATCH_NT, 1) k_scale_small(uint4 *p, size_t s, size_t n, uint32_t k)
+__global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
+    k_scale_small(uint4 *p, size_t s, size_t n, uint32_t k)
 {
     extern __shared__ uint4 smem[];
+    __shared__ uint32_t s_taddr;
+    const int warp = threadIdx.x >> 5;
+    if (warp == 0) tmem_alloc(&s_taddr, 512u);
+    tmem_sync_threads();
     const size_t i = (size_t)blockIdx.x * BATCH_NT + threadIdx.x;
-    if (i >= n) return;
-    SmemTab<BATCH_NT> tab{smem + threadIdx.x};
-    ge_p3 P, h;
-    ld_p3(P, p, s, i);
-    smul_build_table(tab, P);
-    smul_ladder_u32(h, k, tab);
-    st_p3(p, s, i, h);
+    const HybridTab<BATCH_NT> tab{smem + threadIdx.x, tmem_warp_addr(s_taddr, warp, 128u * (uint32_t)(warp >> 2))};
+    if ((size_t)blockIdx.x * BATCH_NT + (size_t)warp * 32 < n) // warp-uniform
+        scale_small_lane(p, s, i, i < n, k, tab);
+    tmem_sync_threads();
+    if (warp == 0) tmem_free(s_taddr, 512u);
 }
 
 int batch_block() { return BATCH_NT; }

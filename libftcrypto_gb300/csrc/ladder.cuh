@@ -59,7 +59,7 @@ template <int NT>
 constexpr int tm_max_regs() { return 16384 / ((NT / 32 + 3) / 4) / 32 / 8 * 8; }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) __maxnreg__(tm_max_regs<NT>()) k_smul_var_tm(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step)
+__global__ void __maxnreg__(tm_max_regs<NT>()) k_smul_var_tm(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step)
 {
     static_assert(NT % 32 == 0 && NT <= 512, "whole warps, at most 4 per lane quarter");
     static_assert(NT <= 512 && (size_t)NT * 512 > 116 * 1024, "one block per SM, 128 columns per warp");

@@ -105,12 +105,14 @@ def test_batch_equals_plain_and_oracle(ft, orc):
 
 def test_scale_small_matches_scale(ft, orc):
     g = synth.rng(32)
-    pts = orc.from_scalars(synth.scalars_mod_L(g, 300), threads=8)
-    for k in (0, 1, 7, 1000, 2**32 - 1):
-        a = ft.Array.from_packed(pts)
-        a.scale_small(k)
-        want = orc.scale(pts, synth.int_to_scalar(k), threads=8)
-        assert (a.to_bytes_folded() == orc.encode(want)).all(), k
+    # 300: one block with a partial warp; 1000: three blocks, a partial last one
+    for n, ks in ((300, (0, 1, 7, 1000, 2**32 - 1)), (1000, (3, 2**31 + 5))):
+        pts = orc.from_scalars(synth.scalars_mod_L(g, n), threads=8)
+        for k in ks:
+            a = ft.Array.from_packed(pts)
+            a.scale_small(k)
+            want = orc.scale(pts, synth.int_to_scalar(k), threads=8)
+            assert (a.to_bytes_folded() == orc.encode(want)).all(), (n, k)
 
 
 def test_batch_rejects_conflicts(ft):
