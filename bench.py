@@ -584,9 +584,7 @@ def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slot
             if q["op"] == "encrypt":
                 out = ft.encrypt(pk, m_pool[o:o + n], r_pool[o:o + n], 1)
             elif q["op"] == "rerand":
-                z = ft.encrypt(pk, np.zeros(n, np.uint64), r_pool[o:o + n], 1)
-                q["c"][0].add(z[0])
-                q["c"][1].add(z[1])
+                ft.rerandomise(q["c"][0], q["c"][1], pk, r_pool[o:o + n])
             elif q["op"] == "smul":
                 q["c"][0].mul(k_pool[o:o + n])
                 q["c"][1].mul(k_pool[o:o + n])

@@ -58,6 +58,26 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
 ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint64_t *d_m,
                             const uint8_t *d_r, size_t n, unsigned plaintext_bits);
 
+/* Re-randomisation: (c1_i, c2_i) += (r_i * B, r_i * pk), a fresh encryption
+ * of zero added in place, so the plaintexts are unchanged and the
+ * ciphertexts unlinkable to the old ones.  r: n 32-byte nonces (host). */
+ft_error ftx_rerandomise(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint8_t *r, size_t n);
+
+/* ftx_rerandomise with the nonces in device memory. */
+ft_error ftx_rerandomise_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint8_t *d_r,
+                                size_t n);
+
+/* Decryption of small plaintexts: m[i] is the j < m_max with
+ * c2_i - sk * c1_i = j * B, or UINT64_MAX where there is none (a plaintext
+ * >= m_max, or not a ciphertext under sk).  The discrete logarithm is a
+ * lookup of the point's canonical encoding in a device table of j * B,
+ * j < m_max, built on first use and kept for the next call with the same
+ * m_max (about 80 bytes per entry).  FT_ERR_BAD_SIZE unless
+ * 1 <= m_max <= FTX_DECRYPT_MAX_M; m: length(c1) entries (host). */
+#define FTX_DECRYPT_MAX_M ((uint64_t)1 << 24)
+ft_error ftx_decrypt(const_ft_ge25519_array c1, const_ft_ge25519_array c2, const uint8_t *sk, uint64_t m_max,
+                     uint64_t *m);
+
 /* Segmented sum over CSR offsets: out is a new array of nseg points with
  * out[s] = sum of src[offsets[s] .. offsets[s+1]) (the identity for an empty
  * segment).  offsets has nseg + 1 int32 entries, non-decreasing, from 0 to

@@ -71,6 +71,9 @@ SIGNATURES = {
     "ftx_mul_device": (I, [P, P, S]),
     "ftx_encrypt": (I, [PP, PP, P, P, P, S, U]),
     "ftx_encrypt_device": (I, [P, P, P, P, P, S, U]),
+    "ftx_rerandomise": (I, [P, P, P, P, S]),
+    "ftx_rerandomise_device": (I, [P, P, P, P, S]),
+    "ftx_decrypt": (I, [P, P, P, ctypes.c_uint64, P]),
     "ftx_segmented_sum_csr": (I, [PP, P, S, P]),
     "ftx_segmented_sum_csr_device": (I, [P, P, S, P]),
     "ftx_reduce_into": (I, [P, S, P]),

@@ -298,6 +298,30 @@ def encrypt_device(c1: Array, c2: Array, pk32, d_m: int, d_r: int, n: int, plain
                                    plaintext_bits))
 
 
+def rerandomise(c1: Array, c2: Array, pk32, r) -> None:
+    """(c1, c2) += Enc(0; r) under pk, in place."""
+    pk = _buf(pk32, np.uint8).reshape(32)
+    rr = _buf(r, np.uint8, 32)
+    check(lib().ftx_rerandomise(c1.handle, c2.handle, _ptr(pk), _ptr(rr), rr.shape[0]))
+
+
+def rerandomise_device(c1: Array, c2: Array, pk32, d_r: int, n: int) -> None:
+    pk = _buf(pk32, np.uint8).reshape(32)
+    check(lib().ftx_rerandomise_device(c1.handle, c2.handle, _ptr(pk), ctypes.c_void_p(d_r), n))
+
+
+DECRYPT_MAX_M = 1 << 24
+NO_PLAINTEXT = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def decrypt(c1: Array, c2: Array, sk32, m_max: int) -> np.ndarray:
+    """Plaintexts j < m_max with c2 - sk*c1 = j*B; NO_PLAINTEXT where none."""
+    sk = _buf(sk32, np.uint8).reshape(32)
+    out = np.empty(len(c1), dtype=np.uint64)
+    check(lib().ftx_decrypt(c1.handle, c2.handle, _ptr(sk), int(m_max), _ptr(out)))
+    return out
+
+
 def segmented_sum_csr(offsets, src: Array) -> Array:
     off = _buf(offsets, np.int32)
     return Array._new(lib().ftx_segmented_sum_csr, _ptr(off), off.size - 1, src.handle)

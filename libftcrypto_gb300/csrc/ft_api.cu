@@ -34,6 +34,8 @@ struct Ctx {
     uint8_t pk_bytes[32];
     uint32_t *pk_table = nullptr; // comb table of the cached public key
     bool pk_valid = false;
+    void *dlog_mem = nullptr;     // decryption table of j*B, j < dlog.m_max
+    ft::DlogTable dlog;
 };
 
 Ctx g;
@@ -233,6 +235,37 @@ ft_error ensure_pk_table(const uint8_t *pk)
     CK(e);
     std::memcpy(g.pk_bytes, pk, 32);
     g.pk_valid = true;
+    return FT_ERR_NO_ERROR;
+}
+
+// the decryption table for m_max, built on the device on first use
+ft_error ensure_dlog(uint64_t m_max)
+{
+    if (g.dlog_mem && g.dlog.m_max == m_max) return FT_ERR_NO_ERROR;
+    dev_free(g.dlog_mem);
+    g.dlog_mem = nullptr;
+    g.dlog = ft::DlogTable{};
+    uint64_t cap = 64;
+    while (cap < 2 * m_max) cap <<= 1;
+    void *mem;
+    CK(dev_alloc(&mem, ft::dlog_table_bytes(cap)));
+    // j*B for j < m_max by the comb, encoded, then inserted
+    void *s;
+    const size_t b_pts = align256(m_max * FT_PLANES_BYTES_PER_POINT), b_js = align256(m_max * 8);
+    cudaError_t e = scratch(&s, b_pts + b_js + align256(m_max * 32));
+    View pts{(uint4 *)s, (size_t)m_max};
+    uint64_t *js = (uint64_t *)((uint8_t *)s + b_pts);
+    uint8_t *enc = (uint8_t *)s + b_pts + b_js;
+    if (e == cudaSuccess) e = ft::iota_u64(js, m_max, g.stream);
+    if (e == cudaSuccess) e = ft::smul_base_small(pts, m_max, js, g.stream);
+    if (e == cudaSuccess) e = ft::encode(enc, pts, m_max, g.stream);
+    if (e == cudaSuccess) e = ft::dlog_build(g.dlog, mem, m_max, cap, enc, g.stream);
+    if (e != cudaSuccess) {
+        dev_free(mem);
+        g.dlog = ft::DlogTable{};
+        return map_err(e);
+    }
+    g.dlog_mem = mem;
     return FT_ERR_NO_ERROR;
 }
 
@@ -867,6 +900,60 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
     }
     *c1 = a;
     *c2 = b;
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_rerandomise_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint8_t *d_r, size_t n)
+{
+    ENSURE_INIT();
+    if (c1->n != n || c2->n != n) return FT_ERR_SIZE_MISMATCH;
+    ft_error err = ensure_pk_table(pk);
+    if (err) return err;
+    CK(ft::rerandomise(ft::view_of(c1), ft::view_of(c2), n, d_r, g.pk_table, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_rerandomise(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint8_t *r, size_t n)
+{
+    ENSURE_INIT();
+    if (c1->n != n || c2->n != n) return FT_ERR_SIZE_MISMATCH;
+    ft_error err = ensure_pk_table(pk);
+    if (err) return err;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, align256(n * 32)));
+    CK(h2d(s, r, n * 32));
+    CK(ft::rerandomise(ft::view_of(c1), ft::view_of(c2), n, (const uint8_t *)s, g.pk_table, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_decrypt(const_ft_ge25519_array c1, const_ft_ge25519_array c2, const uint8_t *sk, uint64_t m_max,
+                     uint64_t *m)
+{
+    ENSURE_INIT();
+    if (m_max == 0 || m_max > FTX_DECRYPT_MAX_M) return FT_ERR_BAD_SIZE;
+    if (c1->n != c2->n) return FT_ERR_SIZE_MISMATCH;
+    ft_error err = ensure_dlog(m_max);
+    if (err) return err;
+    const size_t n = c1->n;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    // D = c2 - sk * c1, encoded, looked up
+    void *s;
+    const size_t b_pts = align256(n * FT_PLANES_BYTES_PER_POINT), b_enc = align256(n * 32), b_m = align256(n * 8);
+    CK(scratch(&s, 2 * b_pts + b_enc + b_m + 256));
+    uint8_t *base = (uint8_t *)s;
+    View t{(uint4 *)base, n}, d{(uint4 *)(base + b_pts), n};
+    uint8_t *enc = base + 2 * b_pts;
+    uint64_t *dm = (uint64_t *)(base + 2 * b_pts + b_enc);
+    uint8_t *dsk = base + 2 * b_pts + b_enc + b_m;
+    CK(h2d(dsk, sk, 32));
+    CK(ft::copy_points(t, ft::view_of(c1), n, g.stream));
+    CK(ft::smul_var(t, n, dsk, 0, g.stream));
+    CK(ft::copy_points(d, ft::view_of(c2), n, g.stream));
+    CK(ft::add(d, t, n, 1, g.stream));
+    CK(ft::encode(enc, d, n, g.stream));
+    CK(ft::dlog_lookup(dm, g.dlog, enc, n, g.stream));
+    CK(d2h(m, dm, n * 8));
     return FT_ERR_NO_ERROR;
 }
 

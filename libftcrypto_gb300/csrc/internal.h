@@ -62,6 +62,22 @@ cudaError_t build_comb_table(uint32_t *d_table, View q, cudaStream_t st);
 // c1 = r*B, c2 = m*B + r*PK; pk_table from build_comb_table
 cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *d_r, const uint64_t *d_m,
                     int m_digits, const uint32_t *d_pk_table, cudaStream_t st);
+// (c1, c2) += (r*B, r*PK): a fresh encryption of zero added in place
+cudaError_t rerandomise(View c1, View c2, size_t n, const uint8_t *d_r, const uint32_t *d_pk_table, cudaStream_t st);
+// discrete-log table of j*B, j < m_max (k_elgamal.cu): open addressing over
+// the canonical encodings, cap slots (a power of two >= 2 m_max)
+struct DlogTable {
+    uint32_t *state = nullptr; // 0 empty, else j + 1
+    uint32_t *enc = nullptr;   // cap x 8 words
+    uint64_t m_max = 0, cap = 0;
+};
+size_t dlog_table_bytes(uint64_t cap);
+// fills a table laid out in `mem` (dlog_table_bytes(cap) bytes) from the
+// encodings of j*B, j < m_max, already at d_enc (m_max x 32 bytes)
+cudaError_t dlog_build(DlogTable &t, void *mem, uint64_t m_max, uint64_t cap, const uint8_t *d_enc, cudaStream_t st);
+// m[i] = j where enc_i (n x 32 bytes) is the encoding of j*B, j < m_max; UINT64_MAX if none
+cudaError_t dlog_lookup(uint64_t *d_m, const DlogTable &t, const uint8_t *d_enc, size_t n, cudaStream_t st);
+cudaError_t iota_u64(uint64_t *d, size_t n, cudaStream_t st);
 // ladder instantiations (k_ladder.cu) and the run-time block-size knob
 cudaError_t ladder_launch_128(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
 cudaError_t ladder_launch_192(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);

@@ -8,7 +8,9 @@
 //                reference uses the variable-base ladder here
 //                (ftcrypto.cu:895-913); the points are the same.
 //   k_encrypt    ElGamal c1 = r*B, c2 = m*B + r*PK with both combs in shared
-//                memory and m*B folded into the PK comb's accumulator.
+//                memory and m*B folded into the PK comb's accumulator; with
+//                ACC the products are added to c1, c2 in place
+//                (re-randomisation: c + Enc(0; r)).
 //   k_comb_table the 32 x 8 affine comb table of a public point (PK).
 #include "internal.h"
 #include "points.cuh"
@@ -93,6 +95,21 @@ __global__ void __launch_bounds__(128) k_comb_base(uint4 *p, size_t s, size_t n,
     }
 }
 
+// dst[i] = h, or dst[i] += h with ACC
+template <bool ACC>
+FT_DEV void put_p3(uint4 *dst, size_t s, size_t i, const ge_p3 &h)
+{
+    if (ACC) {
+        ge_p3 x;
+        ld_p3(x, dst, s, i);
+        ge_addto(x, h);
+        st_p3(dst, s, i, x);
+    } else {
+        st_p3(dst, s, i, h);
+    }
+}
+
+template <bool ACC>
 __global__ void __launch_bounds__(128) k_encrypt(uint4 *c1, size_t s1, uint4 *c2, size_t s2, size_t n, const uint4 *r,
                                                  const uint64_t *m, int mdig, const uint4 *pktab)
 {
@@ -108,7 +125,7 @@ __global__ void __launch_bounds__(128) k_encrypt(uint4 *c1, size_t s1, uint4 *c2
         uint32_t a[8], br[8], bm[8], mw[8];
         load_scalar(a, r, i);
         recode_bias(br, a);
-        uint64_t mv = m[i];
+        uint64_t mv = ACC ? 0 : m[i];
         mw[0] = (uint32_t)mv;
         mw[1] = (uint32_t)(mv >> 32);
 #pragma unroll
@@ -134,11 +151,11 @@ __global__ void __launch_bounds__(128) k_encrypt(uint4 *c1, size_t s1, uint4 *c2
                 comb_row(h, c, parity, row, !use_m && 2 * row + parity == 63, tab);
             if (pass == 0 || pass == 3) ge_mul16(h);
             if (pass == 1) {
-                st_p3(c1, s1, i, h);
+                put_p3<ACC>(c1, s1, i, h);
                 ge_p3_0(h);
             }
         }
-        st_p3(c2, s2, i, h);
+        put_p3<ACC>(c2, s2, i, h);
     }
 }
 
@@ -238,20 +255,33 @@ cudaError_t build_comb_table(uint32_t *d_table, View q, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *r, const uint64_t *m, int mdig,
-                    const uint32_t *pktab, cudaStream_t st)
+template <bool ACC>
+static cudaError_t encrypt_launch(View c1, View c2, size_t n, const uint8_t *r, const uint64_t *m, int mdig,
+                                  const uint32_t *pktab, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
     size_t smem = 2 * COMB_U4 * sizeof(uint4);
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_encrypt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_encrypt<ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_encrypt<<<comb_grid(n), 128, smem, st>>>(c1.p, c1.s, c2.p, c2.s, n, (const uint4 *)r, m, mdig,
-                                               (const uint4 *)pktab);
+    k_encrypt<ACC><<<comb_grid(n), 128, smem, st>>>(c1.p, c1.s, c2.p, c2.s, n, (const uint4 *)r, m, mdig,
+                                                    (const uint4 *)pktab);
     return cudaGetLastError();
+}
+
+cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *r, const uint64_t *m, int mdig,
+                    const uint32_t *pktab, cudaStream_t st)
+{
+    return encrypt_launch<false>(c1, c2, n, r, m, mdig, pktab, st);
+}
+
+// (c1, c2) += (r*B, r*PK)
+cudaError_t rerandomise(View c1, View c2, size_t n, const uint8_t *r, const uint32_t *pktab, cudaStream_t st)
+{
+    return encrypt_launch<true>(c1, c2, n, r, nullptr, 0, pktab, st);
 }
 
 } // namespace ft

@@ -80,7 +80,7 @@ size_t request_bytes(const ftx_request &r)
     const size_t pts = FT_PLANES_BYTES_PER_POINT;
     switch (r.op) {
     case FTX_REQ_ENCRYPT: return 2 * r.n * pts + r.n * 40 + 4096;
-    case FTX_REQ_RERAND: return 2 * r.n * pts + r.n * 40 + 4096;
+    case FTX_REQ_RERAND: return r.n * 32 + 4096;
     case FTX_REQ_SMUL: return r.n * 32 + 4096;
     case FTX_REQ_SEGSUM: return 2 * r.nseg * pts + (r.nseg + 1) * 4 + 2 * ft::segsum_scratch_bytes(r.n) + 8192;
     default: return 0;
@@ -177,18 +177,12 @@ ft_error ftx_server_s::dispatch(Req *q, Slot &sl)
         if (e == cudaSuccess) e = enc(q->res.c1, q->res.c2, r.m, r.plaintext_bits);
         break;
     }
-    case FTX_REQ_RERAND: {
-        ft_ge25519_array z1 = nullptr, z2 = nullptr;
-        e = new_array(&z1, r.n, st);
-        if (e == cudaSuccess) e = new_array(&z2, r.n, st);
-        if (e == cudaSuccess) e = enc(z1, z2, nullptr, 1);
-        if (e == cudaSuccess) e = ft::add(ft::view_of(r.c1), ft::view_of(z1), r.n, 0, st);
-        if (e == cudaSuccess) e = ft::add(ft::view_of(r.c2), ft::view_of(z2), r.n, 0, st);
-        for (ft_ge25519_array z : {z1, z2})
-            if (z) {
-                q->tmp.push_back(z->planes);
-                std::free(z);
-            }
+    case FTX_REQ_RERAND: { // (c1, c2) += Enc(0; r), fused into the encryption kernel
+        void *dr;
+        e = alloc_on(q, &dr, r.n * 32, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dr, r.r, r.n * 32, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = ft::rerandomise(ft::view_of(r.c1), ft::view_of(r.c2), r.n, (const uint8_t *)dr, pk_table, st);
         q->res.c1 = r.c1;
         q->res.c2 = r.c2;
         break;

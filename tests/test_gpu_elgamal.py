@@ -1,0 +1,79 @@
+"""ElGamal helpers beyond the reference's interface (ftx_rerandomise,
+ftx_decrypt): decryption recovers the plaintexts through the device table of
+j*B, re-randomisation adds exactly (r*B, r*PK) (checked against the oracle)
+and leaves the plaintexts unchanged."""
+import numpy as np
+import pytest
+
+from libftcrypto_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def keys(ft, g):
+    sk = synth.scalars_mod_L(g, 1)
+    pk_arr = ft.Array.from_scalars(sk)
+    return sk[0], pk_arr.to_bytes_folded()[0], pk_arr.to_packed()
+
+
+@pytest.mark.parametrize("n", [0, 1, 257, 3000])
+def test_decrypt_roundtrip(ft, n):
+    g = synth.rng(70 + n)
+    sk, pk, _ = keys(ft, g)
+    m = g.integers(0, 1000, size=n, dtype=np.uint64)
+    if n >= 2:
+        m[0], m[1] = 0, 999
+    c1, c2 = ft.encrypt(pk, m, synth.scalars_mod_L(g, n), 10)
+    assert (ft.decrypt(c1, c2, sk, 1000) == m).all()
+
+
+def test_decrypt_out_of_range_wrong_key_and_sums(ft):
+    g = synth.rng(81)
+    sk, pk, _ = keys(ft, g)
+    m = np.array([0, 5, 999, 1000, 1001, 4095], dtype=np.uint64)
+    c1, c2 = ft.encrypt(pk, m, synth.scalars_mod_L(g, m.size), 12)
+    got = ft.decrypt(c1, c2, sk, 1000)
+    assert (got[:3] == m[:3]).all() and (got[3:] == ft.NO_PLAINTEXT).all()
+    other, _, _ = keys(ft, g)  # c2 - sk'*c1 = m*B + r*(sk - sk')*B: no small plaintext
+    assert (ft.decrypt(c1, c2, other, 1000) == ft.NO_PLAINTEXT).all()
+    # a smaller table (rebuilt), then the homomorphic sum under a larger one
+    assert (ft.decrypt(c1, c2, sk, 6)[:2] == m[:2]).all()
+    assert (ft.decrypt(c1, c2, sk, 6)[2:] == ft.NO_PLAINTEXT).all()
+    d1, d2 = ft.encrypt(pk, m, synth.scalars_mod_L(g, m.size), 12)
+    c1.add(d1)
+    c2.add(d2)
+    assert (ft.decrypt(c1, c2, sk, 8192) == 2 * m).all()
+    assert (ft.decrypt(c1, c2, sk, 1) == np.where(m == 0, 0, ft.NO_PLAINTEXT)).all()
+
+
+def test_decrypt_arguments(ft):
+    g = synth.rng(82)
+    sk, pk, _ = keys(ft, g)
+    c1, c2 = ft.encrypt(pk, np.zeros(4, np.uint64), synth.scalars_mod_L(g, 4), 1)
+    for bad in (0, ft.DECRYPT_MAX_M + 1):
+        with pytest.raises(ft.FtError) as e:
+            ft.decrypt(c1, c2, sk, bad)
+        assert e.value.code == 3
+    with pytest.raises(ft.FtError) as e:
+        ft.decrypt(c1, c2.get_range(0, 3, 1), sk, 10)
+    assert e.value.code == 2
+
+
+@pytest.mark.parametrize("n", [1, 300, 2049])
+def test_rerandomise_vs_oracle(ft, orc, n):
+    g = synth.rng(90 + n)
+    sk, pk, pk_packed = keys(ft, g)
+    m = g.integers(0, 256, size=n, dtype=np.uint64)
+    c1, c2 = ft.encrypt(pk, m, synth.scalars_mod_L(g, n), 8)
+    old1, old2 = c1.to_packed(), c2.to_packed()
+    r2 = synth.scalars_mod_L(g, n)
+    ft.rerandomise(c1, c2, pk, r2)
+    want1 = orc.add(old1, orc.from_scalars(r2, threads=8))
+    want2 = orc.add(old2, orc.mul(np.repeat(pk_packed, n, axis=0), r2, threads=8))
+    assert (c1.to_bytes_folded() == orc.encode(want1)).all()
+    assert (c2.to_bytes_folded() == orc.encode(want2)).all()
+    assert (c1.to_bytes_folded() != orc.encode(old1)).any(axis=1).all()
+    assert (ft.decrypt(c1, c2, sk, 256) == m).all()
+    with pytest.raises(ft.FtError) as e:
+        ft.rerandomise(c1, c2, pk, r2[: n - 1] if n > 1 else synth.scalars_mod_L(g, 2))
+    assert e.value.code == 2
