@@ -667,8 +667,8 @@ def run_reference(args):
     kind = "port"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded PCG64)",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64 (the oracle's 4 x 64-bit limbs)", "data": "synthetic (seeded PCG64)",
             "config": {"workload": f"encrypt + per-element scalar-mult, bounded sample of {n} of the "
                                    f"1,048,576 ciphertexts per step", "smul_per_ct": SMUL_PER_CT,
                        "plaintext_bits": 8},
