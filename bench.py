@@ -358,10 +358,9 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     a1, a2 = encrypt_dev(ma)
     b1, b2 = encrypt_dev(mb)
     s1, s2 = a1.get_range(0, n1, 1), a2.get_range(0, n1, 1)
-    s1.add(b1)
-    s2.add(b2)
+    ft.ct_add(s1, s2, b1, b2)
     ok = decrypt_matches(ft, s1, s2, sk[0], ma + mb)
-    ms = timed(ev, lambda: (a1.add(b1), a2.add(b2)), 9, flush)
+    ms = timed(ev, lambda: ft.ct_add(a1, a2, b1, b2), 9, flush)
     out["ct_add_65536"] = {"ct_adds_per_s": n1 / (ms * 1e-3), "ms": ms, "decrypt_check": ok, "l2": "flushed",
                            **roof(2 * n1 * 3 * B_PT, 2 * n1 * W_ALG_PTADD, ms, hbm_peak, imad)}
 

@@ -58,6 +58,13 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
 ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint64_t *d_m,
                             const uint8_t *d_r, size_t n, unsigned plaintext_bits);
 
+/* Ciphertext add / subtract: (c1, c2) += (d1, d2) (resp. -=), element-wise,
+ * both halves in one launch; the points equal ft_add(c1, d1) followed by
+ * ft_add(c2, d2) (or ft_sub), also when arrays alias (then it runs as those
+ * two calls).  Arrays of one length. */
+ft_error ftx_ct_add(ft_ge25519_array c1, ft_ge25519_array c2, const_ft_ge25519_array d1, const_ft_ge25519_array d2);
+ft_error ftx_ct_sub(ft_ge25519_array c1, ft_ge25519_array c2, const_ft_ge25519_array d1, const_ft_ge25519_array d2);
+
 /* Re-randomisation: (c1_i, c2_i) += (r_i * B, r_i * pk), a fresh encryption
  * of zero added in place, so the plaintexts are unchanged and the
  * ciphertexts unlinkable to the old ones.  r: n 32-byte nonces (host). */

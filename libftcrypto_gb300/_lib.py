@@ -71,6 +71,8 @@ SIGNATURES = {
     "ftx_mul_device": (I, [P, P, S]),
     "ftx_encrypt": (I, [PP, PP, P, P, P, S, U]),
     "ftx_encrypt_device": (I, [P, P, P, P, P, S, U]),
+    "ftx_ct_add": (I, [P, P, P, P]),
+    "ftx_ct_sub": (I, [P, P, P, P]),
     "ftx_rerandomise": (I, [P, P, P, P, S]),
     "ftx_rerandomise_device": (I, [P, P, P, P, S]),
     "ftx_decrypt": (I, [P, P, P, ctypes.c_uint64, P]),

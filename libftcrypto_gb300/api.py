@@ -298,6 +298,15 @@ def encrypt_device(c1: Array, c2: Array, pk32, d_m: int, d_r: int, n: int, plain
                                    plaintext_bits))
 
 
+def ct_add(c1: Array, c2: Array, d1: Array, d2: Array) -> None:
+    """(c1, c2) += (d1, d2) in one launch."""
+    check(lib().ftx_ct_add(c1.handle, c2.handle, d1.handle, d2.handle))
+
+
+def ct_sub(c1: Array, c2: Array, d1: Array, d2: Array) -> None:
+    check(lib().ftx_ct_sub(c1.handle, c2.handle, d1.handle, d2.handle))
+
+
 def rerandomise(c1: Array, c2: Array, pk32, r) -> None:
     """(c1, c2) += Enc(0; r) under pk, in place."""
     pk = _buf(pk32, np.uint8).reshape(32)

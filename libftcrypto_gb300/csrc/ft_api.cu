@@ -903,6 +903,34 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
     return FT_ERR_NO_ERROR;
 }
 
+// (c1, c2) +/-= (d1, d2): one launch, or two in the order of ft_add(c1, d1),
+// ft_add(c2, d2) when one half is read or written by the other's update
+static ft_error ct_add_sub(ft_ge25519_array c1, ft_ge25519_array c2, const_ft_ge25519_array d1, const_ft_ge25519_array d2,
+                    int sub)
+{
+    if (c1->n != c2->n || d1->n != c1->n || d2->n != c1->n) return FT_ERR_SIZE_MISMATCH;
+    const size_t n = c1->n;
+    if (c1 == c2 || d2 == c1 || d1 == c2) {
+        CK(ft::add(ft::view_of(c1), ft::view_of(d1), n, sub, g.stream));
+        CK(ft::add(ft::view_of(c2), ft::view_of(d2), n, sub, g.stream));
+        return FT_ERR_NO_ERROR;
+    }
+    CK(ft::add_ct(ft::view_of(c1), ft::view_of(c2), ft::view_of(d1), ft::view_of(d2), n, sub, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_ct_add(ft_ge25519_array c1, ft_ge25519_array c2, const_ft_ge25519_array d1, const_ft_ge25519_array d2)
+{
+    ENSURE_INIT();
+    return ct_add_sub(c1, c2, d1, d2, 0);
+}
+
+ft_error ftx_ct_sub(ft_ge25519_array c1, ft_ge25519_array c2, const_ft_ge25519_array d1, const_ft_ge25519_array d2)
+{
+    ENSURE_INIT();
+    return ct_add_sub(c1, c2, d1, d2, 1);
+}
+
 ft_error ftx_rerandomise_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint8_t *d_r, size_t n)
 {
     ENSURE_INIT();

@@ -32,6 +32,8 @@ inline View view_of(const ft_ge25519_array_s *a, size_t off = 0) { return View{a
 cudaError_t set_zero(View v, size_t n, cudaStream_t st);
 cudaError_t broadcast(View dst, size_t n, View src, cudaStream_t st);
 cudaError_t add(View res, View src, size_t n, int sub, cudaStream_t st);
+// (r1, r2) +/-= (a1, a2) in one launch
+cudaError_t add_ct(View r1, View r2, View a1, View a2, size_t n, int sub, cudaStream_t st);
 cudaError_t neg(View v, size_t n, cudaStream_t st);
 cudaError_t index_nonzero(int64_t *d_out, View v, size_t n, cudaStream_t st);
 cudaError_t equal(int64_t *d_out, View a, View b, size_t n, int invert, cudaStream_t st);

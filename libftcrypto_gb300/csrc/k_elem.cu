@@ -76,6 +76,27 @@ __global__ void __launch_bounds__(128, 4) k_add(uint4 *r, size_t rs, const uint4
     }
 }
 
+// ciphertext add: (r1, r2) += (a1, a2) over one index space of 2n points,
+// so both halves of a ciphertext array share one launch
+__global__ void __launch_bounds__(128, 4) k_add_ct(uint4 *r1, size_t r1s, const uint4 *a1, size_t a1s, uint4 *r2,
+                                                   size_t r2s, const uint4 *a2, size_t a2s, size_t n, int sub)
+{
+    FT_GRID_LOOP(j, 2 * n)
+    {
+        const bool hi = j >= n;
+        const size_t i = hi ? j - n : j;
+        uint4 *r = hi ? r2 : r1;
+        const uint4 *a = hi ? a2 : a1;
+        const size_t rs = hi ? r2s : r1s, as = hi ? a2s : a1s;
+        ge_p3 x, y;
+        ld_p3(x, r, rs, i);
+        ld_p3(y, a, as, i);
+        if (sub) ge_subfrom(x, y);
+        else ge_addto(x, y);
+        st_p3(r, rs, i, x);
+    }
+}
+
 // negates Y and T, as ge25519_neg of ftcrypto.cu:163-167 does
 __global__ void __launch_bounds__(256) k_neg(uint4 *p, size_t s, size_t n)
 {
@@ -504,6 +525,10 @@ __global__ void __launch_bounds__(128) k_validate(const uint4 *p, size_t s, size
 cudaError_t set_zero(View v, size_t n, cudaStream_t st) { FT_LAUNCH(k_set_zero, n, 256, v.p, v.s, n); }
 cudaError_t broadcast(View d, size_t n, View q, cudaStream_t st) { FT_LAUNCH(k_broadcast, n, 256, d.p, d.s, n, q.p, q.s); }
 cudaError_t add(View r, View a, size_t n, int sub, cudaStream_t st) { FT_LAUNCH(k_add, n, 128, r.p, r.s, a.p, a.s, n, sub); }
+cudaError_t add_ct(View r1, View r2, View a1, View a2, size_t n, int sub, cudaStream_t st)
+{
+    FT_LAUNCH(k_add_ct, 2 * n, 128, r1.p, r1.s, a1.p, a1.s, r2.p, r2.s, a2.p, a2.s, n, sub);
+}
 cudaError_t neg(View v, size_t n, cudaStream_t st) { FT_LAUNCH(k_neg, n, 256, v.p, v.s, n); }
 cudaError_t index_nonzero(int64_t *o, View v, size_t n, cudaStream_t st) { FT_LAUNCH(k_index, n, 256, o, v.p, v.s, n); }
 cudaError_t equal(int64_t *o, View a, View b, size_t n, int inv, cudaStream_t st) { FT_LAUNCH(k_equal, n, 128, o, a.p, a.s, b.p, b.s, n, inv); }

@@ -77,3 +77,36 @@ def test_rerandomise_vs_oracle(ft, orc, n):
     with pytest.raises(ft.FtError) as e:
         ft.rerandomise(c1, c2, pk, r2[: n - 1] if n > 1 else synth.scalars_mod_L(g, 2))
     assert e.value.code == 2
+
+
+@pytest.mark.parametrize("n", [0, 1, 1000])
+def test_ct_add_sub_match_ft_add(ft, orc, n):
+    """ftx_ct_add / ftx_ct_sub (one launch over both halves) equal ft_add /
+    ft_sub on each half, also when arrays alias."""
+    g = synth.rng(110 + n)
+    pts = [orc.from_scalars(synth.scalars_mod_L(g, n), threads=8) for _ in range(4)]
+
+    def arrs():
+        return [ft.Array.from_packed(p) for p in pts]
+
+    for op in ("add", "sub"):
+        fn = ft.ct_add if op == "add" else ft.ct_sub
+        for case in ("plain", "d1_is_c1", "d2_is_c1", "c1_is_c2"):
+            c1, c2, d1, d2 = arrs()
+            e1, e2, f1, f2 = arrs()
+            if case == "d1_is_c1":
+                d1, f1 = c1, e1
+            elif case == "d2_is_c1":
+                d2, f2 = c1, e1
+            elif case == "c1_is_c2":
+                c2, e2 = c1, e1
+            fn(c1, c2, d1, d2)
+            getattr(e1, op)(f1)
+            getattr(e2, op)(f2)
+            assert (c1.to_packed() == e1.to_packed()).all(), (op, case)
+            assert (c2.to_packed() == e2.to_packed()).all(), (op, case)
+    if n:
+        c1, c2, d1, d2 = arrs()
+        with pytest.raises(ft.FtError) as e:
+            ft.ct_add(c1, c2, d1.get_range(0, n - 1, 1) if n > 1 else ft.Array.init_scalar(2), d2)
+        assert e.value.code == 2
