@@ -740,7 +740,8 @@ def run_ours(args):
     return 0
 
 
-PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "reduce", "scan", "segsum", "isum", "encode", "decode")
+PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan", "segsum", "isum", "encode", "decode",
+                 "batch")
 
 
 def run_profile(case: str) -> int:
@@ -791,6 +792,26 @@ def run_profile(case: str) -> int:
             keys = g.integers(0, big // 16, big).astype(np.uint64)
             res = ft.Array.init_scalar(big // 16)
             op = lambda: res.reduce_isum(keys, a)  # noqa: E731
+    elif case == "ct_add":  # two arrays of 1,048,576 ciphertexts (1 GB: larger than L2)
+        c1, c2, d1, d2 = (ft.Array.init_point(n, base, k) for k in (3, 5, 7, 9))
+        op = lambda: ft.ct_add(c1, c2, d1, d2)  # noqa: E731
+    elif case == "batch":  # the uneven mix at 512 arrays (~3 M ciphertexts)
+        b = ft.Batch()
+        for w in synth.uneven_mix(g, n_arrays=512):
+            ln = w["len"]
+            c1, c2 = ft.Array.init_point(ln, base, 3), ft.Array.init_point(ln, base, 5)
+            if w["op"] == "add":
+                s = ft.Array.init_point(ln, base, 7)
+                b.add(c1, s)
+                b.add(c2, s)
+            elif w["op"] == "scale":
+                b.scale_small(c1, w["k"])
+                b.scale_small(c2, w["k"])
+            else:
+                nseg = len(w["offsets"]) - 1
+                b.segmented_sum(ft.Array.init_scalar(nseg), w["offsets"], c1)
+                b.segmented_sum(ft.Array.init_scalar(nseg), w["offsets"], c2)
+        op = b.run  # noqa: E731
     elif case == "encode":
         a = ft.Array.init_point(n, base, 1)
         a.mul_device(d_sc.data_ptr(), n)
