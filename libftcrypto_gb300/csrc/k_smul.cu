@@ -109,8 +109,10 @@ FT_DEV void put_p3(uint4 *dst, size_t s, size_t i, const ge_p3 &h)
     }
 }
 
+// four blocks per SM (128 registers, a few spills to L1) rather than three
+// at 166 registers: 15.39 against 15.73 ms for 1,048,576 plaintexts
 template <bool ACC>
-__global__ void __launch_bounds__(128) k_encrypt(uint4 *c1, size_t s1, uint4 *c2, size_t s2, size_t n, const uint4 *r,
+__global__ void __launch_bounds__(128, 4) k_encrypt(uint4 *c1, size_t s1, uint4 *c2, size_t s2, size_t n, const uint4 *r,
                                                  const uint64_t *m, int mdig, const uint4 *pktab)
 {
     extern __shared__ uint4 smem[];
