@@ -415,7 +415,7 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=3):
     """4,096 ciphertext arrays, lengths log-uniform in [1, 65,536], each with
     one op (add 40%, scale by k in [1,1000] 30%, segmented sum of mean-8
     segments 30%): one persistent launch replayed from a CUDA graph against
-    one library call per array (ft_add / ftx_scale_small /
+    one library call per array (ft_add / ftx_scale_bounded /
     ftx_segmented_sum_csr_device, two per ciphertext array)."""
     ev = Ev(st)
     g = synth.rng(SEED + 11)
@@ -443,8 +443,8 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=3):
                 c1.add(ex["s1"])
                 c2.add(ex["s2"])
             elif w["op"] == "scale":
-                c1.scale_small(w["k"])
-                c2.scale_small(w["k"])
+                c1.scale_small(w["k"], w["bits"])
+                c2.scale_small(w["k"], w["bits"])
             else:
                 nseg = len(ex["o1"])
                 ft.segmented_sum_csr_device(ex["o1"], ex["doff"].data_ptr(), nseg, c1)
@@ -457,8 +457,8 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=3):
                 b.add(c1, ex["s1"])
                 b.add(c2, ex["s2"])
             elif w["op"] == "scale":
-                b.scale_small(c1, w["k"])
-                b.scale_small(c2, w["k"])
+                b.scale_small(c1, w["k"], w["bits"])
+                b.scale_small(c2, w["k"], w["bits"])
             else:
                 b.segmented_sum(ex["o1"], w["offsets"], c1)
                 b.segmented_sum(ex["o2"], w["offsets"], c2)
@@ -805,8 +805,8 @@ def run_profile(case: str) -> int:
                 b.add(c1, s)
                 b.add(c2, s)
             elif w["op"] == "scale":
-                b.scale_small(c1, w["k"])
-                b.scale_small(c2, w["k"])
+                b.scale_small(c1, w["k"], w["bits"])
+                b.scale_small(c2, w["k"], w["bits"])
             else:
                 nseg = len(w["offsets"]) - 1
                 b.segmented_sum(ft.Array.init_scalar(nseg), w["offsets"], c1)

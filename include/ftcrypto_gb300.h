@@ -105,6 +105,11 @@ ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_
  * ft_scale with the 32-byte scalar k). */
 ft_error ftx_scale_small(ft_ge25519_array array, uint32_t k);
 
+/* ftx_scale_small for a declared public bound k < 2^bits (1 <= bits <= 32):
+ * (bits + 1) / 4 + 1 windows instead of nine, constant time in k for a given
+ * bits (3 windows for k < 1024).  FT_ERR_BAD_SIZE if k >= 2^bits. */
+ft_error ftx_scale_bounded(ft_ge25519_array array, uint32_t k, unsigned bits);
+
 /* Batched form: record many independent operations on arrays of any
  * lengths, then run them all in one persistent kernel launch replayed from a
  * CUDA graph.  The first ftx_batch_run uploads the work list and captures
@@ -121,6 +126,8 @@ ft_error ftx_batch_create(ftx_batch *batch);
 ft_error ftx_batch_add(ftx_batch batch, ft_ge25519_array res, const_ft_ge25519_array summand);
 /* array[i] = k * array[i], k < 2^32 (as ftx_scale_small) */
 ft_error ftx_batch_scale_small(ftx_batch batch, ft_ge25519_array array, uint32_t k);
+/* array[i] = k * array[i], k < 2^bits (as ftx_scale_bounded) */
+ft_error ftx_batch_scale_bounded(ftx_batch batch, ft_ge25519_array array, uint32_t k, unsigned bits);
 /* out[s] = sum of src[offsets[s] .. offsets[s+1]) for s < nseg; out has
  * length nseg; offsets (host, copied) as for ftx_segmented_sum_csr */
 ft_error ftx_batch_segmented_sum(ftx_batch batch, ft_ge25519_array out, const int32_t *offsets, size_t nseg,

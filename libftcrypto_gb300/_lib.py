@@ -80,9 +80,11 @@ SIGNATURES = {
     "ftx_segmented_sum_csr_device": (I, [P, P, S, P]),
     "ftx_reduce_into": (I, [P, S, P]),
     "ftx_scale_small": (I, [P, ctypes.c_uint32]),
+    "ftx_scale_bounded": (I, [P, ctypes.c_uint32, U]),
     "ftx_batch_create": (I, [PP]),
     "ftx_batch_add": (I, [P, P, P]),
     "ftx_batch_scale_small": (I, [P, P, ctypes.c_uint32]),
+    "ftx_batch_scale_bounded": (I, [P, P, ctypes.c_uint32, U]),
     "ftx_batch_segmented_sum": (I, [P, P, P, S, P]),
     "ftx_batch_run": (I, [P]),
     "ftx_batch_info": (I, [P, PS, PS]),

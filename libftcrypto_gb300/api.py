@@ -237,8 +237,9 @@ class Array:
         s = _buf(scalars, np.uint8, 32)
         check(lib().ft_mul(self._h, _ptr(s), s.shape[0]))
 
-    def scale_small(self, k: int) -> None:
-        check(lib().ftx_scale_small(self._h, int(k)))
+    def scale_small(self, k: int, bits: int = 32) -> None:
+        """self[i] = k * self[i] for k < 2^bits (a public bound)."""
+        check(lib().ftx_scale_bounded(self._h, int(k), int(bits)))
 
     def mul_device(self, d_scalars_ptr: int, n: int) -> None:
         check(lib().ftx_mul_device(self._h, ctypes.c_void_p(d_scalars_ptr), n))
@@ -354,8 +355,8 @@ class Batch:
         check(lib().ftx_batch_add(self._h, res.handle, summand.handle))
         self._keep += [res, summand]
 
-    def scale_small(self, arr: Array, k: int) -> None:
-        check(lib().ftx_batch_scale_small(self._h, arr.handle, int(k)))
+    def scale_small(self, arr: Array, k: int, bits: int = 32) -> None:
+        check(lib().ftx_batch_scale_bounded(self._h, arr.handle, int(k), int(bits)))
         self._keep.append(arr)
 
     def segmented_sum(self, out: Array, offsets, src: Array) -> None:

@@ -1049,12 +1049,15 @@ ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_
     return FT_ERR_NO_ERROR;
 }
 
-ft_error ftx_scale_small(ft_ge25519_array array, uint32_t k)
+ft_error ftx_scale_bounded(ft_ge25519_array array, uint32_t k, unsigned bits)
 {
     ENSURE_INIT();
-    CK(ft::scale_small(ft::view_of(array), array->n, k, g.stream));
+    if (bits < 1 || bits > 32 || (bits < 32 && (k >> bits))) return FT_ERR_BAD_SIZE;
+    CK(ft::scale_small(ft::view_of(array), array->n, k, u32_ladder_windows(bits), g.stream));
     return FT_ERR_NO_ERROR;
 }
+
+ft_error ftx_scale_small(ft_ge25519_array array, uint32_t k) { return ftx_scale_bounded(array, k, 32); }
 
 } // extern "C"
 
@@ -1118,9 +1121,10 @@ ft_error claim(ftx_batch b, const void *w, const void *r)
     return FT_ERR_NO_ERROR;
 }
 
+// scales (longest ladders first), then segmented sums, then adds
 int item_rank(const ft::BatchItem &it)
 {
-    return it.op == ft::BATCH_SCALE ? 0 : (it.op == ft::BATCH_SEG ? 1 : 2);
+    return it.op == ft::BATCH_SCALE ? 9 - (int)it.nwin : (it.op == ft::BATCH_SEG ? 10 : 11);
 }
 
 ft_error batch_upload(ftx_batch b)
@@ -1186,8 +1190,9 @@ ft_error ftx_batch_add(ftx_batch b, ft_ge25519_array res, const_ft_ge25519_array
     return FT_ERR_NO_ERROR;
 }
 
-ft_error ftx_batch_scale_small(ftx_batch b, ft_ge25519_array a, uint32_t k)
+ft_error ftx_batch_scale_bounded(ftx_batch b, ft_ge25519_array a, uint32_t k, unsigned bits)
 {
+    if (bits < 1 || bits > 32 || (bits < 32 && (k >> bits))) return FT_ERR_BAD_SIZE;
     ft_error err = claim(b, a->planes, nullptr);
     if (err) return err;
     const size_t per = (size_t)ft::batch_block();
@@ -1198,9 +1203,15 @@ ft_error ftx_batch_scale_small(ftx_batch b, ft_ge25519_array a, uint32_t k)
         it.dst = a->planes + base;
         it.dst_s = a->cap;
         it.k = k;
+        it.nwin = (uint32_t)u32_ladder_windows(bits);
         b->items.push_back(it);
     }
     return FT_ERR_NO_ERROR;
+}
+
+ft_error ftx_batch_scale_small(ftx_batch b, ft_ge25519_array a, uint32_t k)
+{
+    return ftx_batch_scale_bounded(b, a, k, 32);
 }
 
 ft_error ftx_batch_segmented_sum(ftx_batch b, ft_ge25519_array out, const int32_t *off, size_t nseg,

@@ -8,7 +8,7 @@
 //   the run is short ones (longest-processing-time order).  Item kinds:
 //     ADD    dst[i] += src[i] for count points (count <= 384 x points/thread)
 //     SCALE  dst[i] = k * dst[i], count <= 384 points, one per thread,
-//            constant time in k < 2^32 (smul_ladder_u32)
+//            constant time in k < 2^bits (smul_ladder_u32 in nwin windows)
 //     SEG    dst[s] = sum of src[off[s] .. off[s+1]), count <= 384 segments,
 //            one per thread (segments of the batched workload are short)
 //   The host side (ft_api.cu, ftx_batch_*) captures {counter reset, k_batch}
@@ -29,7 +29,8 @@ namespace ft {
 static constexpr int BATCH_NT = 384;
 
 // k * (point i of p) for the lanes with live set, the identity for the rest
-FT_DEV void scale_small_lane(uint4 *p, size_t s, size_t i, bool live, uint32_t k, const HybridTab<BATCH_NT> &tab)
+FT_DEV void scale_small_lane(uint4 *p, size_t s, size_t i, bool live, uint32_t k, int nwin,
+                             const HybridTab<BATCH_NT> &tab)
 {
     ge_p3 P, h;
     if (live) ld_p3(P, p, s, i);
@@ -37,7 +38,7 @@ FT_DEV void scale_small_lane(uint4 *p, size_t s, size_t i, bool live, uint32_t k
     __syncwarp();
     smul_build_table(tab, P);
     tmem_wait_st();
-    smul_ladder_u32(h, k, tab);
+    smul_ladder_u32(h, k, tab, nwin);
     if (live) st_p3(p, s, i, h);
 }
 
@@ -69,7 +70,7 @@ __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
             }
         } else if (w.op == BATCH_SCALE) {
             if ((uint32_t)(warp * 32) < w.count) // warp-uniform
-                scale_small_lane(w.dst, w.dst_s, tid, (uint32_t)tid < w.count, w.k, tab);
+                scale_small_lane(w.dst, w.dst_s, tid, (uint32_t)tid < w.count, w.k, (int)w.nwin, tab);
         } else { // BATCH_SEG
 #pragma unroll 1
             for (uint32_t sg = tid; sg < w.count; sg += BATCH_NT) {
@@ -92,7 +93,7 @@ __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
 }
 
 __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
-    k_scale_small(uint4 *p, size_t s, size_t n, uint32_t k)
+    k_scale_small(uint4 *p, size_t s, size_t n, uint32_t k, int nwin)
 {
     extern __shared__ uint4 smem[];
     __shared__ uint32_t s_taddr;
@@ -102,7 +103,7 @@ __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
     const size_t i = (size_t)blockIdx.x * BATCH_NT + threadIdx.x;
     const HybridTab<BATCH_NT> tab{smem + threadIdx.x, tmem_warp_addr(s_taddr, warp, 128u * (uint32_t)(warp >> 2))};
     if ((size_t)blockIdx.x * BATCH_NT + (size_t)warp * 32 < n) // warp-uniform
-        scale_small_lane(p, s, i, i < n, k, tab);
+        scale_small_lane(p, s, i, i < n, k, nwin, tab);
     tmem_sync_threads();
     if (warp == 0) tmem_free(s_taddr, 512u);
 }
@@ -132,13 +133,13 @@ cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, c
     return cudaGetLastError();
 }
 
-cudaError_t scale_small(View v, size_t n, uint32_t k, cudaStream_t st)
+cudaError_t scale_small(View v, size_t n, uint32_t k, int nwin, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
     static bool attr = false;
     cudaError_t e = set_smem_attr((const void *)k_scale_small, batch_smem_bytes(), attr);
     if (e != cudaSuccess) return e;
-    k_scale_small<<<(unsigned)((n + BATCH_NT - 1) / BATCH_NT), BATCH_NT, batch_smem_bytes(), st>>>(v.p, v.s, n, k);
+    k_scale_small<<<(unsigned)((n + BATCH_NT - 1) / BATCH_NT), BATCH_NT, batch_smem_bytes(), st>>>(v.p, v.s, n, k, nwin);
     return cudaGetLastError();
 }
 

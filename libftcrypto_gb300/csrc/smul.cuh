@@ -10,6 +10,7 @@
 //       table[i][j] = (j+1) * 256^i * Q, selected in constant time.
 #pragma once
 #include "ge.cuh"
+#include "windows.h"
 
 // Tab: put(k, const ge_cached&), get(k, ge_cached&) for k in [0, 8) and
 // select_fe(f, j, babs, one): coordinate j (0 YplusX, 1 YminusX, 2 Z, 3 T2d)
@@ -138,20 +139,22 @@ FT_DEV void smul_ladder(ge_p3 &h, const uint32_t a[8], const Tab &tab)
     ge_p1p1_to_p3(h, r);
 }
 
-// h = k * P for k < 2^32, constant time in k: the nine signed radix-16
-// digits a 32-bit scalar has under the reference's recoding (digits 9..63
-// are zero), in the same window sequence as smul_ladder, so the point equals
-// smul_ladder's for the 32-byte scalar k.
+// h = k * P for k < 2^32, constant time in k, in nwin signed radix-16
+// windows (digits nwin-1 .. 0 of the reference's recoding, each a table
+// select, an add and four doublings but the last).  The digits of k under
+// the bias sum_{i<nwin} 8 * 16^i are exact when k + bias < 16^nwin, which
+// holds for k < 2^bits with nwin = u32_ladder_windows(bits) (windows.h).
+// The point equals smul_ladder's for the 32-byte scalar k.
 template <class Tab>
-FT_DEV void smul_ladder_u32(ge_p3 &h, uint32_t k, const Tab &tab)
+FT_DEV void smul_ladder_u32(ge_p3 &h, uint32_t k, const Tab &tab, int nwin = 9)
 {
     const uint64_t b = (uint64_t)k + 0x888888888ull; // nibbles 0..8 biased by 8
     ge_p3_0(h);
     ge_p1p1 r;
     ge_p2 s;
-    int d = (int)((b >> 32) & 15u) - 8;
+    int d = (int)((b >> (4 * (nwin - 1))) & 15u) - 8;
 #pragma unroll 1
-    for (int i = 8; i > 0; --i) {
+    for (int i = nwin - 1; i > 0; --i) {
         ge_add_select(r, h, tab, d);
 #pragma unroll 1
         for (int j = 0; j < 4; ++j) {
@@ -164,6 +167,7 @@ FT_DEV void smul_ladder_u32(ge_p3 &h, uint32_t k, const Tab &tab)
     ge_add_select(r, h, tab, d);
     ge_p1p1_to_p3(h, r);
 }
+
 
 FT_DEV void shr8_256(uint32_t c[8])
 {

@@ -75,9 +75,10 @@ def segment_ids(offsets: np.ndarray) -> np.ndarray:
 def uneven_mix(g: np.random.Generator, n_arrays: int = 4096, max_len: int = 65536, seg_mean: int = 8):
     """The uneven batched workload: n_arrays ciphertext arrays with lengths
     floor(exp(U(0, ln max_len))) clamped to [1, max_len], each drawing one op:
-    add (40%), multiply by a scalar uniform in [1, 1000] (30%), or a
-    segmented sum with ~geometric segments of mean seg_mean (30%).
-    Returns a list of dicts {len, op, k | offsets}."""
+    add (40%), multiply by a scalar uniform in [1, 1000] (30%; "bits" = 10
+    is the public bound k < 2^10 of that draw), or a segmented sum with
+    ~geometric segments of mean seg_mean (30%).
+    Returns a list of dicts {len, op, k and bits | offsets}."""
     lens = np.clip(np.floor(np.exp(g.uniform(0.0, np.log(max_len), n_arrays))), 1, max_len).astype(np.int64)
     ops = g.choice(3, size=n_arrays, p=[0.4, 0.3, 0.3])
     out = []
@@ -86,7 +87,7 @@ def uneven_mix(g: np.random.Generator, n_arrays: int = 4096, max_len: int = 6553
         if op == 0:
             out.append({"len": n, "op": "add"})
         elif op == 1:
-            out.append({"len": n, "op": "scale", "k": int(g.integers(1, 1001))})
+            out.append({"len": n, "op": "scale", "k": int(g.integers(1, 1001)), "bits": 10})
         else:
             nseg = max(1, int(round(n / seg_mean)))
             out.append({"len": n, "op": "segsum", "offsets": csr_offsets(g, n, nseg)})

@@ -86,6 +86,17 @@ int hc_mul_hybrid(uint8_t *pts, const uint8_t *scalars, size_t n, int nt)
     else return -1;
     return 0;
 }
+// the small-scalar ladder in the window count for k < 2^bits
+void hc_mul_u32_bits(uint8_t *pts, const uint32_t *k, size_t n, unsigned bits)
+{
+    for (size_t i = 0; i < n; ++i) {
+        ge_p3 p, h; ArrTab tab;
+        ld(p, pts + 128 * i);
+        smul_build_table(tab, p);
+        smul_ladder_u32(h, k[i], tab, u32_ladder_windows(bits));
+        st(pts + 128 * i, h);
+    }
+}
 void hc_mul_u32(uint8_t *pts, const uint32_t *k, size_t n)
 {
     for (size_t i = 0; i < n; ++i) {

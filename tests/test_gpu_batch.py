@@ -41,8 +41,8 @@ def run_plain(ft, work, arrs):
             c1.add(ex["s1"])
             c2.add(ex["s2"])
         elif w["op"] == "scale":
-            c1.scale_small(w["k"])
-            c2.scale_small(w["k"])
+            c1.scale_small(w["k"], w["bits"])
+            c2.scale_small(w["k"], w["bits"])
         else:
             ex["o1"].free()
             ex["o2"].free()
@@ -57,8 +57,8 @@ def build_batch(ft, work, arrs):
             b.add(c1, ex["s1"])
             b.add(c2, ex["s2"])
         elif w["op"] == "scale":
-            b.scale_small(c1, w["k"])
-            b.scale_small(c2, w["k"])
+            b.scale_small(c1, w["k"], w["bits"])
+            b.scale_small(c2, w["k"], w["bits"])
         else:
             b.segmented_sum(ex["o1"], w["offsets"], c1)
             b.segmented_sum(ex["o2"], w["offsets"], c2)
@@ -113,6 +113,31 @@ def test_scale_small_matches_scale(ft, orc):
             a.scale_small(k)
             want = orc.scale(pts, synth.int_to_scalar(k), threads=8)
             assert (a.to_bytes_folded() == orc.encode(want)).all(), (n, k)
+
+
+def test_scale_bounded_windows(ft, orc):
+    """ftx_scale_bounded: (bits + 1) / 4 + 1 windows, exact at the largest k
+    of each bound, and in the batched form; k >= 2^bits and bits outside
+    1..32 are refused."""
+    g = synth.rng(33)
+    pts = orc.from_scalars(synth.scalars_mod_L(g, 500), threads=8)
+    for bits in (1, 3, 7, 10, 11, 16, 31, 32):
+        for k in {(1 << bits) - 1, (1 << bits) // 2, 1}:
+            a = ft.Array.from_packed(pts)
+            a.scale_small(k, bits)
+            want = orc.encode(orc.scale(pts, synth.int_to_scalar(k), threads=8))
+            assert (a.to_bytes_folded() == want).all(), (bits, k)
+            c = ft.Array.from_packed(pts)
+            b = ft.Batch()
+            b.scale_small(c, k, bits)
+            b.run()
+            assert (c.to_bytes_folded() == want).all(), (bits, k)
+            b.free()
+    a = ft.Array.from_packed(pts[:4])
+    for k, bits in ((1024, 10), (2, 1), (1, 0), (1, 33)):
+        with pytest.raises(ft.FtError) as e:
+            a.scale_small(k, bits)
+        assert e.value.code == 3
 
 
 def test_batch_rejects_conflicts(ft):
