@@ -2,6 +2,7 @@
 // kernel translation units (k_*.cu).  Not installed; the public interface is
 // include/ftcrypto.h and include/ftcrypto_gb300.h.
 #pragma once
+#include <atomic>
 #include <cuda_runtime.h>
 #include "windows.h"
 #include <stddef.h>
@@ -22,6 +23,20 @@ struct ft_ge25519_array_s {
 namespace ft {
 
 // A view of n points starting at element `off` of an array.
+// the dynamic shared-memory limit of a kernel, raised on its first launch
+// (concurrent first launches from the serving worker and a caller thread
+// may both set it, which is harmless)
+struct SmemAttr {
+    std::atomic<bool> done{false};
+};
+inline cudaError_t ensure_smem_attr(SmemAttr &a, const void *fn, size_t bytes)
+{
+    if (a.done.load(std::memory_order_acquire)) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) a.done.store(true, std::memory_order_release);
+    return e;
+}
+
 struct View {
     uint4 *p;
     size_t s; // plane stride

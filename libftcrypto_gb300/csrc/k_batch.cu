@@ -112,17 +112,9 @@ int batch_block() { return BATCH_NT; }
 
 size_t batch_smem_bytes() { return ladder_smem_bytes<BATCH_NT>(); }
 
-static cudaError_t set_smem_attr(const void *f, size_t bytes, bool &done)
-{
-    if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess) done = true;
-    return e;
-}
+static SmemAttr g_batch_attr, g_scale_attr;
 
-static bool g_batch_attr = false;
-
-cudaError_t batch_prepare() { return set_smem_attr((const void *)k_batch, batch_smem_bytes(), g_batch_attr); }
+cudaError_t batch_prepare() { return ensure_smem_attr(g_batch_attr, (const void *)k_batch, batch_smem_bytes()); }
 
 cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, cudaStream_t st)
 {
@@ -136,8 +128,7 @@ cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, c
 cudaError_t scale_small(View v, size_t n, uint32_t k, int nwin, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
-    static bool attr = false;
-    cudaError_t e = set_smem_attr((const void *)k_scale_small, batch_smem_bytes(), attr);
+    cudaError_t e = ensure_smem_attr(g_scale_attr, (const void *)k_scale_small, batch_smem_bytes());
     if (e != cudaSuccess) return e;
     k_scale_small<<<(unsigned)((n + BATCH_NT - 1) / BATCH_NT), BATCH_NT, batch_smem_bytes(), st>>>(v.p, v.s, n, k, nwin);
     return cudaGetLastError();

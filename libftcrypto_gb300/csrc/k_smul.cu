@@ -263,12 +263,9 @@ static cudaError_t encrypt_launch(View c1, View c2, size_t n, const uint8_t *r, 
 {
     if (n == 0) return cudaSuccess;
     size_t smem = 2 * COMB_U4 * sizeof(uint4);
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_encrypt<ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static SmemAttr attr;
+    cudaError_t e = ensure_smem_attr(attr, (const void *)k_encrypt<ACC>, smem);
+    if (e != cudaSuccess) return e;
     k_encrypt<ACC><<<comb_grid(n), 128, smem, st>>>(c1.p, c1.s, c2.p, c2.s, n, (const uint4 *)r, m, mdig,
                                                     (const uint4 *)pktab);
     return cudaGetLastError();

@@ -96,13 +96,9 @@ cudaError_t launch_ladder(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_
     const void *fn;
     if constexpr (NT > 256) fn = (const void *)k_smul_var_tm<NT>;
     else fn = (const void *)k_smul_var<NT>;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)ladder_smem_bytes<NT>());
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static SmemAttr attr;
+    cudaError_t e = ensure_smem_attr(attr, fn, ladder_smem_bytes<NT>());
+    if (e != cudaSuccess) return e;
     unsigned grid = (unsigned)((n + NT - 1) / NT);
     if constexpr (NT > 256) k_smul_var_tm<NT><<<grid, NT, ladder_smem_bytes<NT>(), st>>>(p, s, n, sc, sc_step);
     else k_smul_var<NT><<<grid, NT, ladder_smem_bytes<NT>(), st>>>(p, s, n, sc, sc_step);
