@@ -190,6 +190,8 @@ void ftx_server_free(ftx_server server);
 #define FTX_TUNE_LADDER_BLOCK 1  /* variable-base ladder block size: 128, 192, 224 (tables in shared
                                     memory) or 384, 448 (tables half in tensor memory) */
 #define FTX_TUNE_BATCH_ADD_PTS 2 /* batched form: points per thread of an ADD item (1..64) */
+#define FTX_TUNE_SCALE_WINDOW 3  /* window width of the small-scalar ladder (ftx_scale_bounded and the
+                                    batched scale; 2, 3 or 4 bits; a batch takes it at its first run) */
 ft_error ftx_tune(int knob, int value);
 int ftx_tune_get(int knob);
 

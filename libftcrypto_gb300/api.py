@@ -392,6 +392,7 @@ def tune_get(knob: int) -> int:
 
 
 TUNE_LADDER_BLOCK = 1
+TUNE_SCALE_WINDOW = 3
 TUNE_BATCH_ADD_PTS = 2
 
 

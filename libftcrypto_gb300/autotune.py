@@ -9,9 +9,15 @@ Knobs and candidates:
   FTX_TUNE_BATCH_ADD_PTS  points per thread of an ADD item of the batched
                           form: 1, 2, 4, 8, 16 (item granularity against
                           queue overhead)
-The window width of the ladder is not a knob: the reference's 4-bit signed
-window is kept because it fixes the sequence of group operations, which is
-what makes results agree with the reference on every input.
+  FTX_TUNE_SCALE_WINDOW   window width of the small-scalar ladder
+                          (ftx_scale_bounded, batched scales): 2, 3, 4 bits,
+                          timed on scalars below 2^10, the bound of the
+                          batched workload (table of 2, 4 or 8 entries against
+                          the number of windows; the points are the same)
+The window width of the 253-bit variable-base ladder is not a knob: the
+reference's 4-bit signed window is kept there (it is also the minimum of
+field operations for 253-bit scalars, and an 8-entry table per thread is
+what the SM's shared and tensor memory hold).
 
 Each candidate is timed on the device (best of three, synchronised wall
 clock) and the fastest is applied.  Results are cached per GPU model in
@@ -30,8 +36,11 @@ from . import api, synth
 CANDIDATES = {
     api.TUNE_LADDER_BLOCK: (128, 192, 224, 384, 448),
     api.TUNE_BATCH_ADD_PTS: (1, 2, 4, 8, 16),
+    api.TUNE_SCALE_WINDOW: (2, 3, 4),
 }
-NAMES = {api.TUNE_LADDER_BLOCK: "ladder_block", api.TUNE_BATCH_ADD_PTS: "batch_add_pts"}
+NAMES = {api.TUNE_LADDER_BLOCK: "ladder_block", api.TUNE_BATCH_ADD_PTS: "batch_add_pts",
+         api.TUNE_SCALE_WINDOW: "scale_window"}
+SCALE_BITS = 10  # the bound of the batched workload's scalars (k <= 1000)
 
 
 def cache_path() -> str:
@@ -82,6 +91,13 @@ def tune(n_points: int = 1 << 18, seed: int = 7) -> dict:
     best[api.TUNE_BATCH_ADD_PTS] = min(CANDIDATES[api.TUNE_BATCH_ADD_PTS],
                                        key=lambda v: timings[f"batch_add_pts={v}"])
     api.tune(api.TUNE_BATCH_ADD_PTS, best[api.TUNE_BATCH_ADD_PTS])
+    # small-scalar ladder width at the batched workload's bound
+    for v in CANDIDATES[api.TUNE_SCALE_WINDOW]:
+        api.tune(api.TUNE_SCALE_WINDOW, v)
+        timings[f"scale_window={v}"] = _best_of(lambda: work.scale_small(1000, SCALE_BITS))
+    best[api.TUNE_SCALE_WINDOW] = min(CANDIDATES[api.TUNE_SCALE_WINDOW],
+                                      key=lambda v: timings[f"scale_window={v}"])
+    api.tune(api.TUNE_SCALE_WINDOW, best[api.TUNE_SCALE_WINDOW])
     result = {NAMES[k]: v for k, v in best.items()}
     result["timings_s"] = timings
     return result
@@ -98,7 +114,7 @@ def load_or_tune(force: bool = False) -> dict:
                 cache = json.load(f)
         except (OSError, ValueError):
             cache = {}
-    if force or key not in cache:
+    if force or key not in cache or any(name not in cache[key] for name in NAMES.values()):
         cache[key] = tune()
         try:
             os.makedirs(os.path.dirname(path), exist_ok=True)

@@ -138,14 +138,16 @@ struct BatchItem {
     size_t src_s;
     const int32_t *off;   // SEG: count + 1 offsets into src
     uint32_t k;           // SCALE: the scalar
-    uint32_t nwin;        // SCALE: ladder windows, u32_ladder_windows(bits) for k < 2^bits
+    uint32_t bits;        // SCALE: k < 2^bits
+    uint32_t nwin;        // SCALE: ladder windows, u32_ladder_windows(bits, w) at upload
 };
 int batch_block();
 size_t batch_smem_bytes();
-cudaError_t batch_prepare(); // once, outside any stream capture
-cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, cudaStream_t st);
+// w: window width 2..4 of the scale items
+cudaError_t batch_prepare(int w); // once, outside any stream capture
+cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, int w, cudaStream_t st);
 // v[i] = k * v[i] in nwin constant-time windows (k < 2^bits, nwin for bits)
-cudaError_t scale_small(View v, size_t n, uint32_t k, int nwin, cudaStream_t st);
+cudaError_t scale_small(View v, size_t n, uint32_t k, int nwin, int w, cudaStream_t st);
 
 int sm_count();
 

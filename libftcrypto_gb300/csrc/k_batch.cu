@@ -8,7 +8,8 @@
 //   the run is short ones (longest-processing-time order).  Item kinds:
 //     ADD    dst[i] += src[i] for count points (count <= 384 x points/thread)
 //     SCALE  dst[i] = k * dst[i], count <= 384 points, one per thread,
-//            constant time in k < 2^bits (smul_ladder_u32 in nwin windows)
+//            constant time in k < 2^bits (smul_ladder_u32 in nwin windows
+//            of the batch's width W, a template parameter of the kernel)
 //     SEG    dst[s] = sum of src[off[s] .. off[s+1]), count <= 384 segments,
 //            one per thread (segments of the batched workload are short)
 //   The host side (ft_api.cu, ftx_batch_*) captures {counter reset, k_batch}
@@ -28,7 +29,9 @@ namespace ft {
 
 static constexpr int BATCH_NT = 384;
 
-// k * (point i of p) for the lanes with live set, the identity for the rest
+// k * (point i of p) for the lanes with live set, the identity for the
+// rest, in nwin windows of width W (a table of 2^(W-1) entries)
+template <int W>
 FT_DEV void scale_small_lane(uint4 *p, size_t s, size_t i, bool live, uint32_t k, int nwin,
                              const HybridTab<BATCH_NT> &tab)
 {
@@ -36,12 +39,13 @@ FT_DEV void scale_small_lane(uint4 *p, size_t s, size_t i, bool live, uint32_t k
     if (live) ld_p3(P, p, s, i);
     else ge_p3_0(P);
     __syncwarp();
-    smul_build_table(tab, P);
+    smul_build_table<1 << (W - 1)>(tab, P);
     tmem_wait_st();
-    smul_ladder_u32(h, k, tab, nwin);
+    smul_ladder_u32<W>(h, k, tab, nwin);
     if (live) st_p3(p, s, i, h);
 }
 
+template <int W>
 __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
     k_batch(const BatchItem *items, int nitems, int *counter)
 {
@@ -70,7 +74,7 @@ __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
             }
         } else if (w.op == BATCH_SCALE) {
             if ((uint32_t)(warp * 32) < w.count) // warp-uniform
-                scale_small_lane(w.dst, w.dst_s, tid, (uint32_t)tid < w.count, w.k, (int)w.nwin, tab);
+                scale_small_lane<W>(w.dst, w.dst_s, tid, (uint32_t)tid < w.count, w.k, (int)w.nwin, tab);
         } else { // BATCH_SEG
 #pragma unroll 1
             for (uint32_t sg = tid; sg < w.count; sg += BATCH_NT) {
@@ -92,6 +96,7 @@ __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
     if (warp == 0) tmem_free(s_taddr, 512u);
 }
 
+template <int W>
 __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
     k_scale_small(uint4 *p, size_t s, size_t n, uint32_t k, int nwin)
 {
@@ -103,7 +108,7 @@ __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
     const size_t i = (size_t)blockIdx.x * BATCH_NT + threadIdx.x;
     const HybridTab<BATCH_NT> tab{smem + threadIdx.x, tmem_warp_addr(s_taddr, warp, 128u * (uint32_t)(warp >> 2))};
     if ((size_t)blockIdx.x * BATCH_NT + (size_t)warp * 32 < n) // warp-uniform
-        scale_small_lane(p, s, i, i < n, k, nwin, tab);
+        scale_small_lane<W>(p, s, i, i < n, k, nwin, tab);
     tmem_sync_threads();
     if (warp == 0) tmem_free(s_taddr, 512u);
 }
@@ -112,25 +117,45 @@ int batch_block() { return BATCH_NT; }
 
 size_t batch_smem_bytes() { return ladder_smem_bytes<BATCH_NT>(); }
 
-static SmemAttr g_batch_attr, g_scale_attr;
+// the instantiations of a window width w in {2, 3, 4} (index w - 2)
+static const void *const k_batch_fn[3] = {(const void *)k_batch<2>, (const void *)k_batch<3>,
+                                          (const void *)k_batch<4>};
+static const void *const k_scale_fn[3] = {(const void *)k_scale_small<2>, (const void *)k_scale_small<3>,
+                                          (const void *)k_scale_small<4>};
+static SmemAttr g_batch_attr[3], g_scale_attr[3];
 
-cudaError_t batch_prepare() { return ensure_smem_attr(g_batch_attr, (const void *)k_batch, batch_smem_bytes()); }
+static bool width_ok(int w) { return w >= 2 && w <= 4; }
 
-cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, cudaStream_t st)
+cudaError_t batch_prepare(int w)
 {
-    cudaError_t e = batch_prepare();
+    if (!width_ok(w)) return cudaErrorInvalidValue;
+    return ensure_smem_attr(g_batch_attr[w - 2], k_batch_fn[w - 2], batch_smem_bytes());
+}
+
+cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, int w, cudaStream_t st)
+{
+    cudaError_t e = batch_prepare(w);
     if (e != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(d_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
-    k_batch<<<sm_count(), BATCH_NT, batch_smem_bytes(), st>>>(d_items, nitems, d_counter);
+    const unsigned g = (unsigned)sm_count();
+    const size_t sm = batch_smem_bytes();
+    if (w == 2) k_batch<2><<<g, BATCH_NT, sm, st>>>(d_items, nitems, d_counter);
+    else if (w == 3) k_batch<3><<<g, BATCH_NT, sm, st>>>(d_items, nitems, d_counter);
+    else k_batch<4><<<g, BATCH_NT, sm, st>>>(d_items, nitems, d_counter);
     return cudaGetLastError();
 }
 
-cudaError_t scale_small(View v, size_t n, uint32_t k, int nwin, cudaStream_t st)
+cudaError_t scale_small(View v, size_t n, uint32_t k, int nwin, int w, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
-    cudaError_t e = ensure_smem_attr(g_scale_attr, (const void *)k_scale_small, batch_smem_bytes());
+    if (!width_ok(w)) return cudaErrorInvalidValue;
+    cudaError_t e = ensure_smem_attr(g_scale_attr[w - 2], k_scale_fn[w - 2], batch_smem_bytes());
     if (e != cudaSuccess) return e;
-    k_scale_small<<<(unsigned)((n + BATCH_NT - 1) / BATCH_NT), BATCH_NT, batch_smem_bytes(), st>>>(v.p, v.s, n, k, nwin);
+    const unsigned g = (unsigned)((n + BATCH_NT - 1) / BATCH_NT);
+    const size_t sm = batch_smem_bytes();
+    if (w == 2) k_scale_small<2><<<g, BATCH_NT, sm, st>>>(v.p, v.s, n, k, nwin);
+    else if (w == 3) k_scale_small<3><<<g, BATCH_NT, sm, st>>>(v.p, v.s, n, k, nwin);
+    else k_scale_small<4><<<g, BATCH_NT, sm, st>>>(v.p, v.s, n, k, nwin);
     return cudaGetLastError();
 }
 

@@ -41,7 +41,11 @@ struct SmemTab {
         const uint4 *q = b + (size_t)(k * 8 + 2 * j) * NT;
         fe_from_u4(f, q[0], q[NT]);
     }
-    FT_TAB_FN void select_fe(fe &f, int j, uint32_t babs, bool one) const { tab_select_fe(f, *this, j, babs, one); }
+    template <int NE>
+    FT_TAB_FN void select_fe(fe &f, int j, uint32_t babs, bool one) const
+    {
+        tab_select_fe<NE>(f, *this, j, babs, one);
+    }
     FT_TAB_FN void get(int k, ge_cached &c) const
     {
         const uint4 *q = b + (size_t)k * 8 * NT;
@@ -96,17 +100,20 @@ struct HybridTab {
             tmem_ld8(a + 96, c.T2d.v);
         }
     }
+    // entries k < min(NE, 4) from shared memory, 4 <= k < NE from TMEM
+    template <int NE>
     FT_TAB_FN void select_fe(fe &f, int j, uint32_t babs, bool one) const
     {
         if (one) fe_1(f);
         else fe_0(f);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < (NE < 4 ? NE : 4); ++k) {
             const uint4 *q = b + (size_t)(k * 8 + 2 * j) * NT;
             fe e;
             fe_from_u4(e, q[0], q[NT]);
             fe_cmov(f, e, ct_eq_mask(babs, (uint32_t)(k + 1)));
         }
+        if (NE <= 4) return;
         uint32_t r[32];
         tmem_ld32(col + 32u * (uint32_t)j, r);
 #pragma unroll

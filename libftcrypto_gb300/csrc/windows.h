@@ -1,12 +1,27 @@
 // windows.h — window count of the small-scalar ladder (smul_ladder_u32),
 // shared by the device code and the host side that records work items.
 //
-// The signed radix-16 digits of k under the bias sum_{i<nwin} 8 * 16^i are
-// exact when k + bias < 16^nwin.  For k < 2^bits, nwin = (bits + 1) / 4 + 1
-// gives 16^nwin >= 2^(bits+2) while the bias stays below 16^nwin / 2; any
-// 32-bit k takes nine windows.
+// In signed radix 2^w, k is written with m digits in [-2^(w-1), 2^(w-1))
+// by adding the bias sum_{i<m} 2^(w-1) * 2^(w i) and reading w-bit digits
+// minus 2^(w-1); the digits are exact when k + bias < 2^(w m).  For k <
+// 2^bits the ladder takes the smallest such m (nine windows of width 4 for
+// any 32-bit k, three for k < 2^10).
 #pragma once
 
-constexpr int u32_ladder_windows(unsigned bits) { return (int)((bits + 1) / 4) + 1; }
-static_assert(u32_ladder_windows(32) == 9 && u32_ladder_windows(10) == 3 && u32_ladder_windows(7) == 3,
+constexpr unsigned long long u32_ladder_bias(int w, int m)
+{
+    unsigned long long b = 0;
+    for (int i = 0; i < m; ++i) b += (1ull << (w - 1)) << (w * i);
+    return b;
+}
+
+constexpr int u32_ladder_windows(unsigned bits, int w = 4)
+{
+    int m = 1;
+    while (m * w < 62 && (1ull << (w * m)) - u32_ladder_bias(w, m) < (1ull << bits)) ++m;
+    return m;
+}
+
+static_assert(u32_ladder_windows(32) == 9 && u32_ladder_windows(10) == 3 && u32_ladder_windows(7) == 3 &&
+                  u32_ladder_windows(10, 3) == 4 && u32_ladder_windows(10, 2) == 6,
               "window counts");

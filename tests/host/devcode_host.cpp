@@ -18,7 +18,8 @@ struct ArrTab {
     {
         f = j == 0 ? e[k].YplusX : j == 1 ? e[k].YminusX : j == 2 ? e[k].Z : e[k].T2d;
     }
-    void select_fe(fe &f, int j, uint32_t babs, bool one) const { tab_select_fe(f, *this, j, babs, one); }
+    template <int NE>
+    void select_fe(fe &f, int j, uint32_t babs, bool one) const { tab_select_fe<NE>(f, *this, j, babs, one); }
 };
 
 static void base_entry(int row, int k, ge_precomp &e)
@@ -43,6 +44,17 @@ static void mul_hybrid(uint8_t *pts, const uint8_t *scalars, size_t n)
         ld(p, pts + 128 * i); memcpy(a, scalars + 32 * i, 32);
         smul_build_table(tab, p);
         smul_ladder(h, a, tab);
+        st(pts + 128 * i, h);
+    }
+}
+template <int W>
+static void mul_u32_w(uint8_t *pts, const uint32_t *k, size_t n, unsigned bits)
+{
+    for (size_t i = 0; i < n; ++i) {
+        ge_p3 p, h; ArrTab tab;
+        ld(p, pts + 128 * i);
+        smul_build_table<1 << (W - 1)>(tab, p);
+        smul_ladder_u32<W>(h, k[i], tab, u32_ladder_windows(bits, W));
         st(pts + 128 * i, h);
     }
 }
@@ -86,16 +98,15 @@ int hc_mul_hybrid(uint8_t *pts, const uint8_t *scalars, size_t n, int nt)
     else return -1;
     return 0;
 }
-// the small-scalar ladder in the window count for k < 2^bits
-void hc_mul_u32_bits(uint8_t *pts, const uint32_t *k, size_t n, unsigned bits)
+// the small-scalar ladder of window width w (2, 3, 4) in the window count
+// for k < 2^bits
+int hc_mul_u32_bits(uint8_t *pts, const uint32_t *k, size_t n, unsigned bits, int w)
 {
-    for (size_t i = 0; i < n; ++i) {
-        ge_p3 p, h; ArrTab tab;
-        ld(p, pts + 128 * i);
-        smul_build_table(tab, p);
-        smul_ladder_u32(h, k[i], tab, u32_ladder_windows(bits));
-        st(pts + 128 * i, h);
-    }
+    if (w == 2) mul_u32_w<2>(pts, k, n, bits);
+    else if (w == 3) mul_u32_w<3>(pts, k, n, bits);
+    else if (w == 4) mul_u32_w<4>(pts, k, n, bits);
+    else return -1;
+    return 0;
 }
 void hc_mul_u32(uint8_t *pts, const uint32_t *k, size_t n)
 {

@@ -99,20 +99,21 @@ def test_hybrid_table_ladder(hc, orc, nt):
     assert (m == orc.mul(p, sc, threads=8)).all()
 
 
-def test_bounded_small_scalar_ladder(hc, orc):
-    """The small-scalar ladder in (bits + 1) / 4 + 1 windows is exact for
-    every k < 2^bits, including the largest k of each bound (where a window
-    fewer would lose the recoding's carry)."""
-    g = synth.rng(12)
+@pytest.mark.parametrize("w", [2, 3, 4])
+def test_bounded_small_scalar_ladder(hc, orc, w):
+    """The small-scalar ladder of window width w in the window count of
+    windows.h is exact for every k < 2^bits, including the largest k of each
+    bound (where a window fewer would lose the recoding's carry)."""
+    g = synth.rng(12 + w)
     for bits in list(range(1, 17)) + [20, 23, 24, 27, 28, 31, 32]:
         ks = {0, 1, (1 << bits) - 1, (1 << bits) - 2, (1 << bits) // 2}
         ks |= {int(x) for x in g.integers(0, 1 << bits, 3, dtype=np.uint64)}
         ks = np.array(sorted(ks), dtype=np.uint32)
         p = orc.from_scalars(synth.scalars_mod_L(g, ks.size))
         m = p.copy()
-        hc.hc_mul_u32_bits(ptr(m), ptr(ks), ks.size, bits)
+        assert hc.hc_mul_u32_bits(ptr(m), ptr(ks), ks.size, bits, w) == 0
         want = np.stack([orc.scale(p[i:i + 1], synth.int_to_scalar(int(k)))[0] for i, k in enumerate(ks)])
-        assert (orc.encode(m) == orc.encode(want)).all(), bits
+        assert (orc.encode(m) == orc.encode(want)).all(), (w, bits)
 
 
 def test_decode_and_small_comb(hc, orc):

@@ -115,12 +115,15 @@ def test_scale_small_matches_scale(ft, orc):
             assert (a.to_bytes_folded() == orc.encode(want)).all(), (n, k)
 
 
-def test_scale_bounded_windows(ft, orc):
-    """ftx_scale_bounded: (bits + 1) / 4 + 1 windows, exact at the largest k
-    of each bound, and in the batched form; k >= 2^bits and bits outside
-    1..32 are refused."""
-    g = synth.rng(33)
+@pytest.mark.parametrize("width", [2, 3, 4])
+def test_scale_bounded_windows(ft, orc, width):
+    """ftx_scale_bounded at each window width: exact at the largest k of each
+    bound, and in the batched form; k >= 2^bits and bits outside 1..32 are
+    refused."""
+    g = synth.rng(33 + width)
     pts = orc.from_scalars(synth.scalars_mod_L(g, 500), threads=8)
+    before = ft.tune_get(ft.TUNE_SCALE_WINDOW)
+    ft.tune(ft.TUNE_SCALE_WINDOW, width)
     for bits in (1, 3, 7, 10, 11, 16, 31, 32):
         for k in {(1 << bits) - 1, (1 << bits) // 2, 1}:
             a = ft.Array.from_packed(pts)
@@ -133,11 +136,15 @@ def test_scale_bounded_windows(ft, orc):
             b.run()
             assert (c.to_bytes_folded() == want).all(), (bits, k)
             b.free()
+    ft.tune(ft.TUNE_SCALE_WINDOW, before)
     a = ft.Array.from_packed(pts[:4])
     for k, bits in ((1024, 10), (2, 1), (1, 0), (1, 33)):
         with pytest.raises(ft.FtError) as e:
             a.scale_small(k, bits)
         assert e.value.code == 3
+    for bad in (1, 5):
+        with pytest.raises(ft.FtError):
+            ft.tune(ft.TUNE_SCALE_WINDOW, bad)
 
 
 def test_batch_rejects_conflicts(ft):
