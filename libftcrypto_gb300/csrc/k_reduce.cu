@@ -16,11 +16,11 @@
 //            for every length (the reference's kernel indexes its tile sums
 //            wrongly above 256 x grid points, ftcrypto.cu:1512).
 //   segsum   out[s] = sum of src[e] (or src[perm[e]]) for e in
-//            [off[s], off[s+1]): each thread sums 16 consecutive points segment
-//            by segment, writes the segments that begin and end inside it and
-//            records the parts of the segments crossing its edges; a second
-//            kernel joins those parts (k_seg_walk / k_seg_join).  ~1 + 1/16
-//            additions per point.  It serves ft_reduce_isum
+//            [off[s], off[s+1]): each thread sums SEG_K = 32 consecutive points
+//            segment by segment, writes the segments that begin and end inside
+//            it and records the parts of the segments crossing its edges; a
+//            second kernel joins those parts (k_seg_walk / k_seg_join).
+//            ~1 + 1/32 additions per point.  It serves ft_reduce_isum
 //            (ftcrypto.cu:1113-1217, accumulating into res) and the CSR
 //            segmented-sum extension.
 //   keys_to_csr  counting sort of ft_reduce_isum's keys on the device
@@ -373,7 +373,11 @@ __global__ void __launch_bounds__(256) k_seg_empty(uint4 *op, size_t os, const i
     }
 }
 
-static const int SEG_K = 16;
+// points per thread of the walk: 32 rather than 16 halves the threads' fixed
+// costs (the binary search for the first segment, the edge partials, the
+// join): 2.59 -> 2.32 ms for 16,777,216 points in 1,048,576 segments (64 and
+// 128 measure the same as 32; 8 is 3.84 ms)
+static const int SEG_K = 32;
 
 size_t segsum_scratch_bytes(size_t nsrc)
 {
@@ -384,7 +388,7 @@ size_t segsum_scratch_bytes(size_t nsrc)
 // out[s] (+)= sum of src[perm ? perm[e] : e], e in [off[s], off[s+1]):
 // ~1 + 1/SEG_K additions per point, two kernels, no waits between blocks.
 // A segment spanning m threads costs m sequential additions in pass 2
-// (m ~ length / 16; about 1-3 for the benchmark's mean lengths 8-32).
+// (m ~ length / 32; 1-2 for the benchmark's mean lengths 8-32).
 cudaError_t segsum(View out, const int32_t *off, size_t nseg, View src, size_t nsrc, const int32_t *perm,
                    int accumulate, void *scratch, cudaStream_t st)
 {
