@@ -147,6 +147,23 @@ def test_scale_bounded_windows(ft, orc, width):
             ft.tune(ft.TUNE_SCALE_WINDOW, bad)
 
 
+def test_empty_batch_and_arrays(ft):
+    """A batch with no operations, and operations on empty arrays, run and
+    change nothing."""
+    b = ft.Batch()
+    b.run()
+    b.run()
+    b.free()
+    e = ft.Array.init_scalar(0)
+    e.scale_small(5, 3)
+    b = ft.Batch()
+    b.scale_small(e, 5, 3)
+    b.add(ft.Array.init_scalar(0), ft.Array.init_scalar(0))
+    b.run()
+    b.free()
+    assert len(e) == 0
+
+
 def test_batch_rejects_conflicts(ft):
     g = synth.rng(33)
     a = ft.Array.from_scalars(synth.scalars_mod_L(g, 10))

@@ -59,6 +59,14 @@ def test_decrypt_arguments(ft):
     assert e.value.code == 2
 
 
+def test_rerandomise_empty(ft):
+    g = synth.rng(89)
+    _, pk, _ = keys(ft, g)
+    c1, c2 = ft.Array.init_scalar(0), ft.Array.init_scalar(0)
+    ft.rerandomise(c1, c2, pk, synth.scalars_mod_L(g, 0))
+    assert len(c1) == 0 and len(c2) == 0
+
+
 @pytest.mark.parametrize("n", [1, 300, 2049])
 def test_rerandomise_vs_oracle(ft, orc, n):
     g = synth.rng(90 + n)
