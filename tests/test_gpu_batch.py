@@ -147,6 +147,26 @@ def test_scale_bounded_windows(ft, orc, width):
             ft.tune(ft.TUNE_SCALE_WINDOW, bad)
 
 
+def test_scale_small_c_entry_points(ft, orc):
+    """ftx_scale_small and ftx_batch_scale_small (the 32-bit bound) through
+    the C ABI directly."""
+    g = synth.rng(34)
+    pts = orc.from_scalars(synth.scalars_mod_L(g, 100), threads=8)
+    k = 2**32 - 3
+    want = orc.encode(orc.scale(pts, synth.int_to_scalar(k), threads=8))
+    L = ft.api.lib()
+    a = ft.Array.from_packed(pts)
+    ft.check(L.ftx_scale_small(a.handle, k))
+    assert (a.to_bytes_folded() == want).all()
+    a = ft.Array.from_packed(pts)
+    b = ft.Batch()
+    ft.check(L.ftx_batch_scale_small(b._h, a.handle, k))
+    b._keep.append(a)
+    b.run()
+    assert (a.to_bytes_folded() == want).all()
+    b.free()
+
+
 def test_empty_batch_and_arrays(ft):
     """A batch with no operations, and operations on empty arrays, run and
     change nothing."""

@@ -59,6 +59,23 @@ def test_decrypt_arguments(ft):
     assert e.value.code == 2
 
 
+def test_rerandomise_device_matches_host(ft):
+    torch = pytest.importorskip("torch")
+    g = synth.rng(88)
+    sk, pk, _ = keys(ft, g)
+    m = g.integers(0, 4, size=700, dtype=np.uint64)
+    r1, r2 = synth.scalars_mod_L(g, 700), synth.scalars_mod_L(g, 700)
+    a1, a2 = ft.encrypt(pk, m, r1, 2)
+    b1, b2 = ft.encrypt(pk, m, r1, 2)
+    ft.rerandomise(a1, a2, pk, r2)
+    d_r = torch.from_numpy(r2).cuda()
+    torch.cuda.synchronize()
+    ft.rerandomise_device(b1, b2, pk, d_r.data_ptr(), 700)
+    assert (a1.to_bytes_folded() == b1.to_bytes_folded()).all()
+    assert (a2.to_bytes_folded() == b2.to_bytes_folded()).all()
+    assert (ft.decrypt(b1, b2, sk, 4) == m).all()
+
+
 def test_rerandomise_empty(ft):
     g = synth.rng(89)
     _, pk, _ = keys(ft, g)
