@@ -20,7 +20,7 @@ BENCH_LIB = os.path.join(HERE, "libftbench.so")  # bench.py's integer-pipe peak 
 # (source, object, extra defines): k_ladder.cu is compiled once per block size
 LADDER_BLOCKS = (128, 192, 224, 384, 448)  # > 256: tables half in TMEM
 SOURCES = [(s, s.replace(".cu", ".o"), []) for s in ("ft_api.cu", "k_elem.cu", "k_smul.cu", "k_reduce.cu",
-                                                     "k_noalloc.cu", "k_batch.cu", "k_elgamal.cu", "serve.cu")]
+                                                     "k_noalloc.cu", "k_batch.cu", "k_elgamal.cu", "k_encrypt.cu", "serve.cu")]
 SOURCES += [("k_ladder.cu", f"k_ladder_{nt}.o", [f"-DFT_LADDER_NT={nt}"]) for nt in LADDER_BLOCKS]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--extended-lambda"]

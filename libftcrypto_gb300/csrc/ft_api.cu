@@ -32,7 +32,7 @@ struct Ctx {
     long long *d_status = nullptr; // one device word for "last bad index"
     ft_error last_void = FT_ERR_NO_ERROR;
     uint8_t pk_bytes[32];
-    uint32_t *pk_table = nullptr; // comb table of the cached public key
+    uint32_t *pk_table = nullptr; // encryption tables of B and of the cached public key
     bool pk_valid = false;
     void *dlog_mem = nullptr;     // decryption table of j*B, j < dlog.m_max
     ft::DlogTable dlog;
@@ -217,12 +217,11 @@ ft_error status_read(int64_t *res)
     return FT_ERR_NO_ERROR;
 }
 
-ft_error ensure_pk_table(const uint8_t *pk)
+// the encryption tables of B and of the public key pk (32-byte folded
+// encoding) into d_tables (ENC_TABLES_BYTES), queued on the library stream
+ft_error build_key_tables(uint32_t *d_tables, const uint8_t *pk)
 {
-    if (g.pk_valid && std::memcmp(g.pk_bytes, pk, 32) == 0) return FT_ERR_NO_ERROR;
-    g.pk_valid = false;
-    if (!g.pk_table) CK(dev_alloc((void **)&g.pk_table, 32 * 8 * 24 * sizeof(uint32_t)));
-    ft_ge25519_array q;
+    ft_ge25519_array q, bq;
     int64_t bad = -1;
     ft_error err = ft_array_from_bytes_folded(&bad, &q, pk, 32);
     if (err) return err;
@@ -230,9 +229,25 @@ ft_error ensure_pk_table(const uint8_t *pk)
         ft_array_free(q);
         return FT_ERR_INVALID_POINT;
     }
-    cudaError_t e = ft::build_comb_table(g.pk_table, ft::view_of(q), g.stream);
+    const uint64_t one = 1;
+    if ((err = ft_array_from_small_scalars(&bq, &one, 1))) {
+        ft_array_free(q);
+        return err;
+    }
+    cudaError_t e = ft::build_enc_tables(d_tables, ft::view_of(bq), ft::view_of(q), g.stream);
     ft_array_free(q);
+    ft_array_free(bq);
     CK(e);
+    return FT_ERR_NO_ERROR;
+}
+
+ft_error ensure_pk_table(const uint8_t *pk)
+{
+    if (g.pk_valid && std::memcmp(g.pk_bytes, pk, 32) == 0) return FT_ERR_NO_ERROR;
+    g.pk_valid = false;
+    if (!g.pk_table) CK(dev_alloc((void **)&g.pk_table, ft::ENC_TABLES_BYTES));
+    ft_error err = build_key_tables(g.pk_table, pk);
+    if (err) return err;
     std::memcpy(g.pk_bytes, pk, 32);
     g.pk_valid = true;
     return FT_ERR_NO_ERROR;
@@ -855,7 +870,7 @@ ft_error ftx_mul_device(ft_ge25519_array array, const uint8_t *d_scalars, size_t
     return FT_ERR_NO_ERROR;
 }
 
-static int m_digits(unsigned bits) { return (int)((bits + 3) / 4) + 1; }
+static int m_digits(unsigned bits) { return ft::enc_m_digits(bits); }
 
 ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint64_t *d_m,
                             const uint8_t *d_r, size_t n, unsigned bits)
@@ -1075,27 +1090,26 @@ namespace ft {
 
 cudaMemPool_t host_pool() { return g.pool; }
 
-// comb table of a public key for a server (cudaMalloc'd; the server frees it)
+// encryption tables of a public key for a server (cudaMalloc'd; the server
+// frees them)
 ft_error ftx_server_pk_table(const uint8_t *pk, uint32_t **table)
 {
-    ft_ge25519_array q;
-    int64_t bad = -1;
-    ft_error err = ft_array_from_bytes_folded(&bad, &q, pk, 32);
-    if (err) return err;
-    if (bad >= 0) {
-        ft_array_free(q);
-        return FT_ERR_INVALID_POINT;
-    }
-    cudaError_t e = cudaMalloc((void **)table, 32 * 8 * 24 * sizeof(uint32_t));
-    if (e == cudaSuccess) e = build_comb_table(*table, view_of(q), g.stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
-    ft_array_free(q);
+    *table = nullptr;
+    cudaError_t e = cudaMalloc((void **)table, ENC_TABLES_BYTES);
     if (e != cudaSuccess) {
-        if (*table) cudaFree(*table);
         *table = nullptr;
         return map_err(e);
     }
-    return FT_ERR_NO_ERROR;
+    ft_error err = build_key_tables(*table, pk);
+    if (!err) {
+        e = cudaStreamSynchronize(g.stream);
+        if (e != cudaSuccess) err = map_err(e);
+    }
+    if (err) {
+        cudaFree(*table);
+        *table = nullptr;
+    }
+    return err;
 }
 
 } // namespace ft
