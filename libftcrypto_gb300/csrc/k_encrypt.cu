@@ -42,15 +42,6 @@ __host__ __device__ constexpr uint32_t enc_bias_word(int w)
     return x;
 }
 
-// a * b + c on the multiply-add pipe (b is a 0/1 indicator here; the asm
-// keeps the compiler from rewriting the product as a select)
-FT_DEV uint32_t imad(uint32_t a, uint32_t b, uint32_t c)
-{
-    uint32_t r;
-    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
-    return r;
-}
-
 FT_DEV void shr5_288(uint32_t c[9])
 {
 #pragma unroll
@@ -104,17 +95,17 @@ FT_DEV void enc_select(ge_precomp &t, int d, const uint4 *row)
             fe_from_u4(e2, q[4], q[5]);
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
-                b.yplusx.v[i] = imad(e0.v[i], ind, b.yplusx.v[i]);
-                b.yminusx.v[i] = imad(e1.v[i], ind, b.yminusx.v[i]);
-                b.xy2d.v[i] = imad(e2.v[i], ind, b.xy2d.v[i]);
+                b.yplusx.v[i] = imad_u32(e0.v[i], ind, b.yplusx.v[i]);
+                b.yminusx.v[i] = imad_u32(e1.v[i], ind, b.yminusx.v[i]);
+                b.xy2d.v[i] = imad_u32(e2.v[i], ind, b.xy2d.v[i]);
             }
         }
     }
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        t.yplusx.v[i] = imad(b.yplusx.v[i], 1u, a.yplusx.v[i]);
-        t.yminusx.v[i] = imad(b.yminusx.v[i], 1u, a.yminusx.v[i]);
-        t.xy2d.v[i] = imad(b.xy2d.v[i], 1u, a.xy2d.v[i]);
+        t.yplusx.v[i] = imad_u32(b.yplusx.v[i], 1u, a.yplusx.v[i]);
+        t.yminusx.v[i] = imad_u32(b.yminusx.v[i], 1u, a.yminusx.v[i]);
+        t.xy2d.v[i] = imad_u32(b.xy2d.v[i], 1u, a.xy2d.v[i]);
     }
     const uint32_t nm = 0u - bneg;
     fe nt;
