@@ -34,6 +34,7 @@ struct Ctx {
     uint8_t pk_bytes[32];
     uint32_t *pk_table = nullptr; // encryption tables of B and of the cached public key
     bool pk_valid = false;
+    uint32_t *b_table = nullptr;  // radix-32 comb table of B (fixed-base products)
     void *dlog_mem = nullptr;     // decryption table of j*B, j < dlog.m_max
     ft::DlogTable dlog;
 };
@@ -221,7 +222,7 @@ ft_error status_read(int64_t *res)
 // encoding) into d_tables (ENC_TABLES_BYTES), queued on the library stream
 ft_error build_key_tables(uint32_t *d_tables, const uint8_t *pk)
 {
-    ft_ge25519_array q, bq;
+    ft_ge25519_array q;
     int64_t bad = -1;
     ft_error err = ft_array_from_bytes_folded(&bad, &q, pk, 32);
     if (err) return err;
@@ -229,14 +230,9 @@ ft_error build_key_tables(uint32_t *d_tables, const uint8_t *pk)
         ft_array_free(q);
         return FT_ERR_INVALID_POINT;
     }
-    const uint64_t one = 1;
-    if ((err = ft_array_from_small_scalars(&bq, &one, 1))) {
-        ft_array_free(q);
-        return err;
-    }
-    cudaError_t e = ft::build_enc_tables(d_tables, ft::view_of(bq), ft::view_of(q), g.stream);
+    cudaError_t e = cudaMemcpyAsync(d_tables, g.b_table, ft::ENC_TABLE_WORDS * 4, cudaMemcpyDeviceToDevice, g.stream);
+    if (e == cudaSuccess) e = ft::build_enc_table(d_tables + ft::ENC_TABLE_WORDS, ft::view_of(q), g.stream);
     ft_array_free(q);
-    ft_array_free(bq);
     CK(e);
     return FT_ERR_NO_ERROR;
 }
@@ -272,7 +268,7 @@ ft_error ensure_dlog(uint64_t m_max)
     uint64_t *js = (uint64_t *)((uint8_t *)s + b_pts);
     uint8_t *enc = (uint8_t *)s + b_pts + b_js;
     if (e == cudaSuccess) e = ft::iota_u64(js, m_max, g.stream);
-    if (e == cudaSuccess) e = ft::smul_base_small(pts, m_max, js, g.stream);
+    if (e == cudaSuccess) e = ft::smul_base_small(pts, m_max, js, g.b_table, g.stream);
     if (e == cudaSuccess) e = ft::encode(enc, pts, m_max, g.stream);
     if (e == cudaSuccess) e = ft::dlog_build(g.dlog, mem, m_max, cap, enc, g.stream);
     if (e != cudaSuccess) {
@@ -335,6 +331,22 @@ ft_error ft_crypto_init(void)
     CK(cudaMemPoolSetAttribute(g.pool, cudaMemPoolAttrReleaseThreshold, &thr));
     g.device = dev;
     CK(cudaMallocFromPoolAsync((void **)&g.d_status, 256, g.pool, g.stream));
+    // the comb table of B, from B's encoding (y = 4/5, x even)
+    {
+        uint8_t benc[32];
+        std::memset(benc, 0x66, 32);
+        benc[0] = 0x58;
+        void *s;
+        CK(dev_alloc((void **)&g.b_table, ft::ENC_TABLE_WORDS * 4));
+        CK(dev_alloc(&s, align256(FT_PLANES_BYTES_PER_POINT) + 256));
+        ft::View bp{(uint4 *)s, 1};
+        uint8_t *d_enc = (uint8_t *)s + align256(FT_PLANES_BYTES_PER_POINT);
+        CK(cudaMemcpyAsync(d_enc, benc, 32, cudaMemcpyHostToDevice, g.stream));
+        CK(ft::decode(bp, d_enc, 1, g.d_status, g.stream));
+        CK(ft::build_enc_table(g.b_table, bp, g.stream));
+        CK(cudaStreamSynchronize(g.stream)); // benc is on the stack
+        dev_free(s);
+    }
     CK(cudaStreamSynchronize(g.stream));
     g.inited = true;
     return FT_ERR_NO_ERROR;
@@ -359,7 +371,7 @@ ft_error ft_array_init_scalar(ft_ge25519_array *array, size_t n, const uint8_t *
         void *s;
         CK(scratch(&s, 256));
         CK(h2d(s, scalar, 32));
-        CK(ft::smul_base(ft::view_of(a), 1, (const uint8_t *)s, 0, g.stream));
+        CK(ft::smul_base(ft::view_of(a), 1, (const uint8_t *)s, 0, g.b_table, g.stream));
         CK(ft::broadcast(ft::view_of(a, 1), n - 1, ft::view_of(a), g.stream));
         return FT_ERR_NO_ERROR;
     });
@@ -587,7 +599,7 @@ ft_error ft_array_from_scalars(ft_ge25519_array *array, const uint8_t *scalars, 
         void *s;
         CK(scratch(&s, align256(n * 32)));
         CK(h2d(s, scalars, n * 32));
-        CK(ft::smul_base(ft::view_of(a), n, (const uint8_t *)s, 1, g.stream));
+        CK(ft::smul_base(ft::view_of(a), n, (const uint8_t *)s, 1, g.b_table, g.stream));
         return FT_ERR_NO_ERROR;
     });
 }
@@ -600,7 +612,7 @@ ft_error ft_array_from_small_scalars(ft_ge25519_array *array, const uint64_t *sm
         void *s;
         CK(scratch(&s, align256(n * 8)));
         CK(h2d(s, small, n * 8));
-        CK(ft::smul_base_small(ft::view_of(a), n, (const uint64_t *)s, g.stream));
+        CK(ft::smul_base_small(ft::view_of(a), n, (const uint64_t *)s, g.b_table, g.stream));
         return FT_ERR_NO_ERROR;
     });
 }
@@ -870,7 +882,7 @@ ft_error ftx_mul_device(ft_ge25519_array array, const uint8_t *d_scalars, size_t
     return FT_ERR_NO_ERROR;
 }
 
-static int m_digits(unsigned bits) { return ft::enc_m_digits(bits); }
+static int m_digits(unsigned bits) { return enc_digits(bits); }
 
 ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t *pk, const uint64_t *d_m,
                             const uint8_t *d_r, size_t n, unsigned bits)

@@ -235,65 +235,9 @@ FT_DEV uint32_t ct_eq_mask(uint32_t a, uint32_t b)
     return 0u - ((x - 1u) >> 31); // all ones iff a == b (a, b < 2^31)
 }
 
-// t = sign(d) * |d| * P from entries[k] = (k+1) * P, identity when |d| is 0
-// or above 8.  Every entry is read and merged under a mask; no address or
-// branch depends on d.
-template <class Get>
-FT_DEV void select_cached(ge_cached &t, int d, Get get)
-{
-    uint32_t bneg = (uint32_t)d >> 31;
-    uint32_t babs = (uint32_t)((d ^ -(int)bneg) + (int)bneg);
-    ge_cached_0(t);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        ge_cached e;
-        get(k, e);
-        uint32_t m = ct_eq_mask(babs, (uint32_t)(k + 1));
-        fe_cmov(t.YplusX, e.YplusX, m);
-        fe_cmov(t.YminusX, e.YminusX, m);
-        fe_cmov(t.Z, e.Z, m);
-        fe_cmov(t.T2d, e.T2d, m);
-    }
-    uint32_t nm = 0u - bneg;
-    fe nt;
-    fe_neg(nt, t.T2d);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        uint32_t sw = (t.YplusX.v[k] ^ t.YminusX.v[k]) & nm;
-        t.YplusX.v[k] ^= sw;
-        t.YminusX.v[k] ^= sw;
-    }
-    fe_cmov(t.T2d, nt, nm);
-}
-
-template <class Get>
-FT_DEV void select_precomp(ge_precomp &t, int d, Get get)
-{
-    uint32_t bneg = (uint32_t)d >> 31;
-    uint32_t babs = (uint32_t)((d ^ -(int)bneg) + (int)bneg);
-    ge_precomp_0(t);
-    // the entry loop stays rolled: unrolled, the comb's loop body outgrows
-    // the instruction cache (rolled: 5.6% faster encryption, measured)
-#pragma unroll 1
-    for (int k = 0; k < 8; ++k) {
-        ge_precomp e;
-        get(k, e);
-        uint32_t m = ct_eq_mask(babs, (uint32_t)(k + 1));
-        fe_cmov(t.yplusx, e.yplusx, m);
-        fe_cmov(t.yminusx, e.yminusx, m);
-        fe_cmov(t.xy2d, e.xy2d, m);
-    }
-    uint32_t nm = 0u - bneg;
-    fe nt;
-    fe_neg(nt, t.xy2d);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        uint32_t sw = (t.yplusx.v[k] ^ t.yminusx.v[k]) & nm;
-        t.yplusx.v[k] ^= sw;
-        t.yminusx.v[k] ^= sw;
-    }
-    fe_cmov(t.xy2d, nt, nm);
-}
+// (the selections that use it: ge_add_select in smul.cuh, enc_select in
+// enc_comb.cuh, each reading every entry and merging under masks, with no
+// address or branch depending on the digit)
 
 // ---- signed radix-16 digits (the recoding of sodium_ge.cu:693-708)
 //

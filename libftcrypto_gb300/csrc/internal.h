@@ -73,18 +73,16 @@ cudaError_t validate(View v, size_t n, long long *d_bad, cudaStream_t st);
 // ---- scalar multiplication (k_smul.cu)
 // per-element (sc_step = 1) or broadcast (sc_step = 0) 32-byte scalars
 cudaError_t smul_var(View v, size_t n, const uint8_t *d_scalars, int sc_step, cudaStream_t st);
-cudaError_t smul_base(View v, size_t n, const uint8_t *d_scalars, int sc_step, cudaStream_t st);
-cudaError_t smul_base_small(View v, size_t n, const uint64_t *d_small, cudaStream_t st);
-// ---- encryption (k_encrypt.cu): a single-pass comb in signed radix 32 over
-// tables of (j+1) * 32^row * Q, j < ENC_ENTRIES, row < ENC_ROWS (affine,
+// a_i * B by the radix-32 comb over B's table (btab, ENC_TABLE_WORDS words)
+cudaError_t smul_base(View v, size_t n, const uint8_t *d_scalars, int sc_step, const uint32_t *btab, cudaStream_t st);
+cudaError_t smul_base_small(View v, size_t n, const uint64_t *d_small, const uint32_t *btab, cudaStream_t st);
+// ---- fixed-base products (k_encrypt.cu): the radix-32 comb (enc_comb.cuh)
+// over tables of (j+1) * 32^row * Q, j < ENC_ENTRIES, row < ENC_ROWS (affine,
 // 24 words per entry); the encryption tables are B's followed by PK's
-constexpr int ENC_ROWS = 52, ENC_ENTRIES = 16;
 constexpr size_t ENC_TABLE_WORDS = (size_t)ENC_ROWS * ENC_ENTRIES * 24;
 constexpr size_t ENC_TABLES_BYTES = 2 * ENC_TABLE_WORDS * 4;
-// B's and PK's tables from element 0 of b and of pk
-cudaError_t build_enc_tables(uint32_t *d_tables, View b, View pk, cudaStream_t st);
-// radix-32 digits of a plaintext below 2^bits (bits <= 64)
-int enc_m_digits(unsigned bits);
+// the table of the point at element 0 of q
+cudaError_t build_enc_table(uint32_t *d_table, View q, cudaStream_t st);
 // c1 = r*B, c2 = m*B + r*PK
 cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *d_r, const uint64_t *d_m,
                     int m_digits, const uint32_t *d_tables, cudaStream_t st);

@@ -167,7 +167,7 @@ ft_error ftx_server_s::dispatch(Req *q, Slot &sl)
             x = hm ? cudaMemcpyAsync(dm, hm, r.n * 8, cudaMemcpyHostToDevice, st) : cudaMemsetAsync(dm, 0, r.n * 8, st);
         if (x == cudaSuccess)
             x = ft::encrypt(ft::view_of(a), ft::view_of(b), r.n, (const uint8_t *)dr, (const uint64_t *)dm,
-                            ft::enc_m_digits(bits), pk_table, st);
+                            enc_digits(bits), pk_table, st);
         return x;
     };
     switch (r.op) {

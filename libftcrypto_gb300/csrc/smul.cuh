@@ -5,9 +5,9 @@
 //       sodium_ge.cu:650-731): table (k+1)*P for k < 8 built in the same
 //       order, 63 x {select, add, 4 doublings} + final add.  The table lives
 //       wherever the caller's accessor puts it (shared memory in the kernels).
-//   comb_accumulate : the fixed-base comb of ge25519_scalarmult_base
-//       (sodium_ge.cu:743-792) over a 32 x 8 affine table
-//       table[i][j] = (j+1) * 256^i * Q, selected in constant time.
+//   smul_ladder_u32 : the same ladder for scalars under a public bound, in
+//       fewer (and optionally narrower) windows.
+// The fixed-base comb is in enc_comb.cuh.
 #pragma once
 #include "ge.cuh"
 #include "windows.h"
@@ -85,7 +85,8 @@ FT_DEV void tab_select_fe(fe &f, const Tab &tab, int j, uint32_t babs, bool one)
 }
 
 // r = p + d * P for a signed digit d in [-NE, NE], where tab holds (k+1)*P:
-// select_cached followed by ge_add (the same field operations on the same
+// the reference's cmov8_cached select (sodium_ge.cu:490-511) followed by
+// ge_add (the same field operations on the same
 // values), with each coordinate of the entry selected just before the
 // multiplication that uses it, so that only two selected coordinates are
 // live at a time.
@@ -179,60 +180,3 @@ FT_DEV void smul_ladder_u32(ge_p3 &h, uint32_t k, const Tab &tab, int nwin = 9)
     ge_p1p1_to_p3(h, r);
 }
 
-FT_DEV void shr8_256(uint32_t c[8])
-{
-#pragma unroll
-    for (int k = 0; k < 7; ++k) c[k] = (c[k] >> 8) | (c[k + 1] << 24);
-    c[7] >>= 8;
-}
-
-// h += sum over rows r < nrows of digit(2r + parity) * table[r], where the
-// digits come from the biased recoding b (see recode_bias).
-// Get: get(row, k, ge_precomp&) returns (k+1) * 256^row * Q.
-template <class Get>
-FT_DEV void comb_accumulate(ge_p3 &h, const uint32_t b[8], int parity, int nrows, Get get)
-{
-    uint32_t c[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) c[k] = b[k];
-    ge_p1p1 r;
-    ge_precomp t;
-#pragma unroll 1
-    for (int row = 0; row < nrows; ++row) {
-        int i = 2 * row + parity;
-        int d = (int)((c[0] >> (4 * parity)) & 15u) - (i == 63 ? 0 : 8);
-        shr8_256(c);
-        select_precomp(t, d, [&](int k, ge_precomp &e) { get(row, k, e); });
-        ge_madd(r, h, t);
-        ge_p1p1_to_p3(h, r);
-    }
-}
-
-// h = 16 * h through the doubling sequence of sodium_ge.cu:778-785
-FT_DEV void ge_mul16(ge_p3 &h)
-{
-    ge_p1p1 r;
-    ge_p2 s;
-    ge_p3_dbl(r, h);
-    ge_p1p1_to_p2(s, r);
-    ge_p2_dbl(r, s);
-    ge_p1p1_to_p2(s, r);
-    ge_p2_dbl(r, s);
-    ge_p1p1_to_p2(s, r);
-    ge_p2_dbl(r, s);
-    ge_p1p1_to_p3(h, r);
-}
-
-// h = a * Q by the comb (ge25519_scalarmult_base, sodium_ge.cu:743-792),
-// restricted to the first `ndigits` radix-16 digits (64 for a full scalar;
-// fewer when a is publicly known to be small).
-template <class Get>
-FT_DEV void comb_mul(ge_p3 &h, const uint32_t a[8], int ndigits, Get get)
-{
-    uint32_t b[8];
-    recode_bias(b, a);
-    ge_p3_0(h);
-    comb_accumulate(h, b, 1, ndigits / 2, get);
-    ge_mul16(h);
-    comb_accumulate(h, b, 0, (ndigits + 1) / 2, get);
-}

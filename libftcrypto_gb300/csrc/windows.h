@@ -25,3 +25,20 @@ constexpr int u32_ladder_windows(unsigned bits, int w = 4)
 static_assert(u32_ladder_windows(32) == 9 && u32_ladder_windows(10) == 3 && u32_ladder_windows(7) == 3 &&
                   u32_ladder_windows(10, 3) == 4 && u32_ladder_windows(10, 2) == 6,
               "window counts");
+
+// The radix-32 fixed-base comb (enc_comb.cuh): ENC_ROWS rows of ENC_ENTRIES
+// entries (j+1) * 32^row * Q, and the rows a scalar below 2^bits needs
+// (bits <= 256): the smallest d with a + sum_{i<d} 16 * 32^i < 32^d for every
+// a < 2^bits, i.e. 15 * 32^d + 16 >= 31 * 2^bits.
+constexpr int ENC_ROWS = 52, ENC_ENTRIES = 16;
+
+constexpr int enc_digits(unsigned bits)
+{
+    int d = 1;
+    // 5d >= bits + 2 always suffices; 5d = bits + 1 only when 2^bits <= 16
+    while (5 * d < (int)bits + 2 && !(5 * d == (int)bits + 1 && bits <= 4)) ++d;
+    return d;
+}
+static_assert(enc_digits(256) == 52 && enc_digits(253) == 51 && enc_digits(64) == 14 && enc_digits(8) == 2 &&
+                  enc_digits(4) == 1 && enc_digits(3) == 1 && enc_digits(5) == 2,
+              "comb rows");

@@ -3,9 +3,7 @@
 // tests/test_devcode_host.py to compare with the oracle.  TEST HARNESS ONLY.
 #include <string.h>
 #include "../../libftcrypto_gb300/csrc/ladder_tab.cuh"
-#define FT_TABLE_QUAL static const
-#define FT_WANT_BASE_COMB
-#include "../../libftcrypto_gb300/csrc/base_table.inc"
+#include "../../libftcrypto_gb300/csrc/enc_comb.cuh"
 
 static void ld(ge_p3 &p, const uint8_t *s) { memcpy(p.X.v, s, 32); memcpy(p.Y.v, s + 32, 32); memcpy(p.Z.v, s + 64, 32); memcpy(p.T.v, s + 96, 32); }
 static void st(uint8_t *s, const ge_p3 &p) { memcpy(s, p.X.v, 32); memcpy(s + 32, p.Y.v, 32); memcpy(s + 64, p.Z.v, 32); memcpy(s + 96, p.T.v, 32); }
@@ -22,13 +20,6 @@ struct ArrTab {
     void select_fe(fe &f, int j, uint32_t babs, bool one) const { tab_select_fe<NE>(f, *this, j, babs, one); }
 };
 
-static void base_entry(int row, int k, ge_precomp &e)
-{
-    const uint32_t *w = FT_BASE_COMB_INIT + (row * 8 + k) * 24;
-    memcpy(e.yplusx.v, w, 32);
-    memcpy(e.yminusx.v, w + 8, 32);
-    memcpy(e.xy2d.v, w + 16, 32);
-}
 
 // the ladder over the tables of the tensor-memory kernel (block size nt,
 // 384 or 448): point i is run as thread i % nt of a block, with that
@@ -118,15 +109,35 @@ void hc_mul_u32(uint8_t *pts, const uint32_t *k, size_t n)
         st(pts + 128 * i, h);
     }
 }
-void hc_comb(uint8_t *pts, const uint8_t *scalars, size_t n, int ndigits)
+// a_i * Q by the radix-32 comb in nrows rows over the 52 x 16 table of Q
+// (built here by enc_table_entry, kept for the next call with the same Q)
+void hc_enc_comb(uint8_t *pts, const uint8_t *scalars, size_t n, int nrows, const uint8_t *q128)
 {
+    static uint4 tab[ENC_ROWS * ENC_ENTRIES * 6];
+    static uint8_t tq[128];
+    static bool have = false;
+    if (!have || memcmp(tq, q128, 128) != 0) {
+        ge_p3 Q;
+        ld(Q, q128);
+        for (int t = 0; t < ENC_ROWS * ENC_ENTRIES; ++t) enc_table_entry(tab + 6 * t, Q, t / ENC_ENTRIES, t % ENC_ENTRIES);
+        memcpy(tq, q128, 128);
+        have = true;
+    }
     for (size_t i = 0; i < n; ++i) {
-        ge_p3 h; uint32_t a[8];
+        ge_p3 h; uint32_t a[8], c[9];
         memcpy(a, scalars + 32 * i, 32);
-        comb_mul(h, a, ndigits, base_entry);
+        if (nrows == ENC_ROWS) {
+            uint32_t ar[8];
+            enc_ref_scalar(ar, a);
+            memcpy(a, ar, 32);
+        }
+        enc_recode(c, a, nrows);
+        ge_p3_0(h);
+        for (int row = 0; row < nrows; ++row) enc_comb_row(h, c, tab + (size_t)row * ENC_ENTRIES * 6);
         st(pts + 128 * i, h);
     }
 }
+int hc_enc_digits(unsigned bits) { return enc_digits(bits); }
 void hc_encode(uint8_t *out, const uint8_t *pts, size_t n)
 {
     for (size_t i = 0; i < n; ++i) {

@@ -76,7 +76,8 @@ def test_group_and_smul(hc, orc):
     om = orc.mul(p1, sc)
     assert (m == om).all()  # same formula sequence: identical coordinates
     c = np.zeros_like(p1)
-    hc.hc_comb(ptr(c), ptr(sc), n, 64)
+    base = orc.from_scalars(synth.int_to_scalar(1)[None])
+    hc.hc_enc_comb(ptr(c), ptr(sc), n, 52, ptr(base))  # the radix-32 comb, 52 rows
     assert (orc.encode(c) == orc.encode(p1)).all()
     e = np.zeros((n, 32), np.uint8)
     hc.hc_encode(ptr(e), ptr(om), n)
@@ -129,8 +130,16 @@ def test_decode_and_small_comb(hc, orc):
     m = np.array([0, 1, 255, 2**32, 2**64 - 1] + list(range(7, 22)), dtype=np.uint64)
     small = orc.small_to_scalars(m)
     c = np.zeros((len(m), 128), np.uint8)
-    hc.hc_comb(ptr(c), ptr(small), len(m), 17)
+    base = orc.from_scalars(synth.int_to_scalar(1)[None])
+    rows = hc.hc_enc_digits(64)
+    assert rows == 14
+    hc.hc_enc_comb(ptr(c), ptr(small), len(m), rows, ptr(base))  # uint64 values: 14 rows
     assert (orc.encode(c) == orc.encode(orc.from_scalars(small))).all()
+    # a full-width scalar and the largest 256-bit one need all 52 rows
+    big = np.stack([synth.int_to_scalar(2**256 - 1), synth.int_to_scalar(2**255 + 12345)])
+    cb = np.zeros((2, 128), np.uint8)
+    hc.hc_enc_comb(ptr(cb), ptr(big), 2, 52, ptr(base))
+    assert (orc.encode(cb) == orc.encode(orc.from_scalars(big))).all()
 
 
 def test_short_ladder_matches_full(hc, orc):

@@ -185,6 +185,25 @@ def test_scale_and_edge_scalars(ft, orc):
         assert (A.to_bytes_folded() == orc.encode(orc.scale(a, s))).all(), v
 
 
+def test_fixed_base_edge_scalars(ft, orc):
+    """from_scalars and encryption at scalars the reference's recoding
+    truncates (top digit above 8, from ~9 * 2^252) and around them: the
+    radix-32 comb reproduces the reference's points."""
+    g = synth.rng(12)
+    vals = [0, 1, 2, synth.L - 1, synth.L, 2**252, 8 * 2**252 + 5, 9 * 2**252 - 1, 9 * 2**252,
+            2**255 - 1, 2**255, 2**255 + 12345, 2**256 - 2**252, 2**256 - 1]
+    s = np.stack([synth.int_to_scalar(v) for v in vals] + list(synth.scalars_mod_L(g, 50)))
+    want = orc.encode(orc.from_scalars(s, threads=8))
+    assert (ft.Array.from_scalars(s).to_bytes_folded() == want).all()
+    sk = synth.scalars_mod_L(g, 1)
+    pk = ft.Array.from_scalars(sk).to_bytes_folded()[0]
+    m = g.integers(0, 256, size=len(s), dtype=np.uint64)
+    c1, c2 = ft.encrypt(pk, m, s, 8)
+    o1, o2 = orc.encrypt(pk, m, s, threads=8)
+    assert (c1.to_bytes_folded() == orc.encode(o1)).all()
+    assert (c2.to_bytes_folded() == orc.encode(o2)).all()
+
+
 def test_constructors(ft, orc):
     g = synth.rng(9)
     s = synth.scalars_mod_L(g, 300)
