@@ -204,6 +204,28 @@ def test_fixed_base_edge_scalars(ft, orc):
     assert (c2.to_bytes_folded() == orc.encode(o2)).all()
 
 
+def test_export_into_pinned_memory(ft, orc):
+    """Exports into pinned (mapped) host memory, written by the conversion
+    kernels directly, equal the exports into pageable memory; an unaligned
+    pinned buffer takes the copying path."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    g = synth.rng(13)
+    n = 1000
+    a = ft.Array.from_scalars(synth.scalars_mod_L(g, n))
+    L = ft.api.lib()
+    for fn, width in ((L.ft_array_to_bytes, 160), (L.ft_array_to_bytes_folded, 32), (L.ft_array_to_bytes_affine, 64)):
+        want = np.zeros(n * width, np.uint8)
+        ft.check(fn(want.ctypes.data_as(ctypes.c_void_p), want.size, a.handle))
+        for off in (0, 1):
+            pin = torch.zeros(n * width + 16, dtype=torch.uint8).pin_memory()
+            ptr = ctypes.c_void_p(pin.data_ptr() + off)
+            ft.check(fn(ptr, n * width, a.handle))
+            got = pin.numpy()[off:off + n * width]
+            assert (got == want).all(), (width, off)
+    assert (want.reshape(n, 64)[:, :32] != 0).any()
+
+
 def test_constructors(ft, orc):
     g = synth.rng(9)
     s = synth.scalars_mod_L(g, 300)
