@@ -8,6 +8,7 @@
 // nothing here exits the process.
 #include <algorithm>
 #include <atomic>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -131,8 +132,13 @@ cudaError_t d2h(void *dst, const void *src, size_t bytes)
     return cudaStreamSynchronize(g.stream);
 }
 
+// arrays whose byte sizes (160 per point at most, in exports) overflow size_t
+// can never be allocated; refusing them keeps every size product exact
+bool too_long(size_t n) { return n > SIZE_MAX / 256; }
+
 ft_error arr_new(ft_ge25519_array *out, size_t n)
 {
+    if (too_long(n)) return FT_ERR_OUT_OF_MEMORY;
     auto *a = (ft_ge25519_array_s *)std::malloc(sizeof(ft_ge25519_array_s));
     if (!a) return FT_ERR_OUT_OF_MEMORY;
     a->n = n;
@@ -151,6 +157,7 @@ ft_error arr_new(ft_ge25519_array *out, size_t n)
 // first `keep` points of the old one
 ft_error arr_realloc(ft_ge25519_array a, size_t cap, size_t keep)
 {
+    if (too_long(cap)) return FT_ERR_OUT_OF_MEMORY;
     uint4 *np = nullptr;
     CK(dev_alloc((void **)&np, cap * FT_PLANES_BYTES_PER_POINT));
     cudaError_t e = ft::copy_points(View{np, cap}, ft::view_of(a), std::min(keep, cap), g.stream);
@@ -459,7 +466,7 @@ ft_error ft_array_assign_to_range(ft_ge25519_array array, size_t start, size_t s
     if ((stop - start) / step > src->n) return FT_ERR_SIZE_MISMATCH;
     // the reference writes src[i] to start + i*step for every i < length(src)
     // with start + i*step < stop (ftcrypto.cu:468-479)
-    size_t count = std::min(src->n, (stop - start + step - 1) / step);
+    size_t count = std::min(src->n, (stop - start - 1) / step + 1);
     if (count == 0) return FT_ERR_NO_ERROR;
     if (start + (count - 1) * step >= array->n) return FT_ERR_OUT_OF_BOUNDS;
     CK(ft::scatter_range(ft::view_of(array), ft::view_of(src), start, step, count, g.stream));
@@ -1168,6 +1175,13 @@ int item_rank(const ft::BatchItem &it)
 
 ft_error batch_upload(ftx_batch b)
 {
+    // a failed upload may be retried: start from no device state
+    dev_free(b->d_items);
+    dev_free(b->d_offs);
+    dev_free(b->d_counter);
+    b->d_items = nullptr;
+    b->d_offs = nullptr;
+    b->d_counter = nullptr;
     b->w = g_scale_w;
     for (auto &it : b->items)
         if (it.op == ft::BATCH_SCALE) it.nwin = (uint32_t)u32_ladder_windows(it.bits, b->w);
@@ -1175,14 +1189,16 @@ ft_error batch_upload(ftx_batch b)
     std::stable_sort(b->items.begin(), b->items.end(),
                      [](const ft::BatchItem &x, const ft::BatchItem &y) { return item_rank(x) < item_rank(y); });
     CK(dev_alloc((void **)&b->d_offs, std::max<size_t>(b->offs.size(), 1) * sizeof(int32_t)));
-    for (auto &it : b->items)
+    // the device copy holds offsets pointers; the host list keeps indices
+    std::vector<ft::BatchItem> dev_items = b->items;
+    for (auto &it : dev_items)
         if (it.op == ft::BATCH_SEG) it.off = b->d_offs + (uintptr_t)it.off;
     CK(dev_alloc((void **)&b->d_items, std::max<size_t>(b->items.size(), 1) * sizeof(ft::BatchItem)));
     CK(dev_alloc((void **)&b->d_counter, 256));
     if (!b->offs.empty())
         CK(cudaMemcpyAsync(b->d_offs, b->offs.data(), b->offs.size() * 4, cudaMemcpyHostToDevice, g.stream));
     if (!b->items.empty())
-        CK(cudaMemcpyAsync(b->d_items, b->items.data(), b->items.size() * sizeof(ft::BatchItem),
+        CK(cudaMemcpyAsync(b->d_items, dev_items.data(), dev_items.size() * sizeof(ft::BatchItem),
                            cudaMemcpyHostToDevice, g.stream));
     CK(cudaStreamSynchronize(g.stream));
     CK(ft::batch_prepare(b->w));

@@ -271,6 +271,10 @@ def test_gather_scatter_delete(ft, orc):
     want = ea.copy()
     want[[4, 9, 14, 19]] = ea[40:44]
     assert (C.to_bytes_folded() == want).all()
+    # a step past the range writes the first point only (no overflow in the count)
+    C.assign_to_range(7, 9, 2**64 - 1, upload(ft, a[45:47]))
+    want[7] = ea[45]
+    assert (C.to_bytes_folded() == want).all()
     D = upload(ft, a)
     D.delete_subset([5, 5, 0, 49, 100])
     keep = [i for i in range(50) if i not in (0, 5, 49)]
@@ -294,6 +298,12 @@ def test_set_length_mux_compare(ft, orc):
     A.set_length(10)  # at most half: reallocated
     A.set_length(12)
     assert (A.to_bytes_folded() == np.concatenate([ea[:10], np.tile(zero, (2, 1))])).all()
+    # lengths whose byte sizes overflow are refused before any allocation
+    for bad in (lambda: A.set_length(2**60), lambda: ft.Array.init_scalar(2**60)):
+        with pytest.raises(ft.FtError) as e:
+            bad()
+        assert e.value.code == 1
+    assert len(A) == 12
     cond = g.integers(0, 2, 40).astype(np.int64)
     M = upload(ft, a)
     M.mux(cond, upload(ft, b))
