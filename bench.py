@@ -45,9 +45,9 @@ METRIC = "EC scalar-mults/s & ciphertext adds/s on 1 GB300 (bit-exact); served p
 UNIT = "EC scalar-mults/s"
 N_CT = 1 << 20
 SMUL_PER_CT = 4
-# Algorithmic work in 32x32->64-bit products (the unit of the IMAD.WIDE peak),
-# the survey's unit: every field multiplication or squaring counts as one
-# 8 x 8-word schoolbook, 64 products.  The CT variable-base ladder
+# Algorithmic work in 32x32->64-bit products (the unit of the IMAD.WIDE peak):
+# every field multiplication or squaring counts as one 8 x 8-word
+# schoolbook, 64 products.  The CT variable-base ladder
 # (sodium_ge.cu:650-731) is 2,340 of them (1,316 M + 1,024 S: 48 M + 16 S
 # for the table, 63 x (20 M + 16 S) for the windows, 8 M for the last add);
 # a point addition is 9 M.

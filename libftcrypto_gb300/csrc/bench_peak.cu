@@ -2,7 +2,7 @@
 // libftbench.so, separate from the product library).
 //
 // Measures 32x32->64-bit multiply-accumulate throughput (IMAD.WIDE: the
-// operation the survey's algorithmic unit counts, 64 per field
+// operation the roofline's algorithmic unit counts, 64 per field
 // multiplication): 8 independent accumulators per thread, each
 // acc = lo32(acc) * m + acc, so no product can be strength-reduced away.
 #include <cuda_runtime.h>
