@@ -152,7 +152,7 @@ void ftx_batch_free(ftx_batch batch);
  * must stay valid until its result is returned; arrays of a request must not
  * be used elsewhere until then.  Results are bit-identical to the same
  * request run alone. */
-#define FTX_REQ_ENCRYPT 1 /* (c1, c2) = Enc(m; r): n plaintexts < 2^bits, n nonces */
+#define FTX_REQ_ENCRYPT 1 /* (c1, c2) = Enc(m; r): n plaintexts < 2^bits (checked), n nonces */
 #define FTX_REQ_RERAND 2  /* (c1, c2) += Enc(0; r) */
 #define FTX_REQ_SMUL 3    /* (c1, c2) = k_i * (c1, c2), n 32-byte scalars, constant time */
 #define FTX_REQ_SEGSUM 4  /* new (c1, c2) of nseg segment sums of the given arrays */
@@ -182,6 +182,7 @@ ft_error ftx_server_submit(ftx_server server, const ftx_request *req, uint64_t *
 ft_error ftx_server_wait(ftx_server server, uint64_t ticket, ftx_result *result);
 /* bytes of the budget in use and requests queued / running */
 ft_error ftx_server_stats(ftx_server server, size_t *bytes_in_use, size_t *queued, size_t *running);
+/* waits for every request; frees the new arrays of results never collected */
 void ftx_server_free(ftx_server server);
 
 /* Launch-shape knobs, set by the autotuner (libftcrypto_gb300/autotune.py)

@@ -361,7 +361,12 @@ ft_error ftx_server_submit(ftx_server s, const ftx_request *req, uint64_t *ticke
 {
     const ftx_request &r = *req;
     if (r.op < FTX_REQ_ENCRYPT || r.op > FTX_REQ_SEGSUM) return FT_ERR_BAD_SIZE;
-    if (r.op == FTX_REQ_ENCRYPT && (r.plaintext_bits < 1 || r.plaintext_bits > 64)) return FT_ERR_BAD_SIZE;
+    if (r.op == FTX_REQ_ENCRYPT) {
+        if (r.plaintext_bits < 1 || r.plaintext_bits > 64) return FT_ERR_BAD_SIZE;
+        if (r.m && r.plaintext_bits < 64) // the comb reads only the digits of the bound
+            for (size_t i = 0; i < r.n; ++i)
+                if (r.m[i] >> r.plaintext_bits) return FT_ERR_BAD_SIZE;
+    }
     if (r.op != FTX_REQ_ENCRYPT && (!r.c1 || !r.c2 || r.c1->n != r.n || r.c2->n != r.n)) return FT_ERR_SIZE_MISMATCH;
     if (r.op == FTX_REQ_SEGSUM) {
         if (r.n >= (size_t)INT32_MAX || r.offsets[0] != 0 || (size_t)r.offsets[r.nseg] != r.n) return FT_ERR_BAD_SIZE;
@@ -427,7 +432,16 @@ void ftx_server_free(ftx_server s)
         }
         if (sl.lib_done) cudaEventDestroy(sl.lib_done);
     }
-    for (auto &kv : s->reqs) delete kv.second;
+    // requests whose results were never collected: their new arrays are
+    // nobody's, so they go with the server (the worker has drained them all)
+    for (auto &kv : s->reqs) {
+        Req *q = kv.second;
+        if (q->finished && !q->res.err && (q->r.op == FTX_REQ_ENCRYPT || q->r.op == FTX_REQ_SEGSUM)) {
+            ft_array_free(q->res.c1);
+            ft_array_free(q->res.c2);
+        }
+        delete q;
+    }
     if (s->pk_table) cudaFree(s->pk_table);
     delete s;
 }

@@ -96,3 +96,19 @@ def test_budget_admission(ft, orc):
         srv.submit_encrypt(np.zeros(2 * n, np.uint64), synth.scalars_mod_L(g, 2 * n), 1)
     assert e.value.code == 7  # larger than the whole budget
     srv.close()
+
+
+def test_submit_checks_and_close_with_results_pending(ft, orc):
+    g = synth.rng(43)
+    pk = orc.encode(orc.from_scalars(synth.scalars_mod_L(g, 1)))[0]
+    srv = ft.Server(pk, 1 << 30, slots=2)
+    r = synth.scalars_mod_L(g, 4)
+    with pytest.raises(ft.FtError) as e:  # a plaintext above its stated bound
+        srv.submit_encrypt(np.array([0, 1, 2, 1], np.uint64), r, 1)
+    assert e.value.code == 3
+    t = srv.submit_encrypt(np.array([0, 1, 1, 0], np.uint64), r, 1)
+    want = folded(ft.encrypt(pk, np.array([0, 1, 1, 0], np.uint64), r, 1))
+    assert (folded(srv.wait(t)[:2]) == want).all()
+    for _ in range(3):  # never collected: freed with the server
+        srv.submit_encrypt(synth.plaintexts(g, 1000, 1), synth.scalars_mod_L(g, 1000), 1)
+    srv.close()
