@@ -114,12 +114,18 @@ int set_ladder_block(int nt);
 // ---- reductions (k_reduce.cu)
 size_t reduce_scratch_bytes(size_t n);
 cudaError_t reduce(View out, View src, size_t n, void *d_scratch, cudaStream_t st);
-// scan: per-thread sums of SCAN_K points, recursively, down to one block
-constexpr size_t SCAN_K = 16; // 32 and 64 measured slower (1.61, 2.04 against 1.48 ms at 4M points)
-constexpr size_t SCAN_SMALL_MAX = 4096;
+// scan: per-thread sums of scan_level_k(n) points, recursively, down to one
+// block.  16 points per thread where the level fills the GPU (32 and 64
+// measured slower: 1.61, 2.04 against 1.48 ms at 4M points); 4 on the
+// latency-bound lower levels, whose cost is the chain of additions in one
+// thread.
+constexpr size_t SCAN_SMALL_MAX = 1024;
+constexpr size_t scan_level_k(size_t n) { return n > ((size_t)1 << 18) ? 16 : 4; }
 constexpr size_t scan_scratch_points(size_t n)
 {
-    return n <= SCAN_SMALL_MAX ? 0 : (n + SCAN_K - 1) / SCAN_K + scan_scratch_points((n + SCAN_K - 1) / SCAN_K);
+    return n <= SCAN_SMALL_MAX ? 0
+                               : (n + scan_level_k(n) - 1) / scan_level_k(n) +
+                                     scan_scratch_points((n + scan_level_k(n) - 1) / scan_level_k(n));
 }
 size_t scan_scratch_bytes(size_t n);
 cudaError_t scan(View v, size_t n, int exclusive, void *d_scratch, cudaStream_t st);

@@ -8,10 +8,11 @@
 //            input point (the reference's tree does the same count but with
 //            most threads idle at the upper levels and 160-byte AoS loads).
 //   scan     inclusive / exclusive prefix (ft_array_scan / ft_array_prescan;
-//            ftcrypto.cu:1474-1586): per-thread sums of SCAN_K = 16 consecutive
-//            points, an exclusive scan of those sums by the same routine (one
-//            block once at most 4096 remain), then each thread rescans its 16
-//            points from its prefix.  ~2 + 2/16 additions per point, one
+//            ftcrypto.cu:1474-1586): per-thread sums of K consecutive points
+//            (16 on levels that fill the GPU, 4 below), an exclusive scan of
+//            those sums by the same routine (one block once at most 1,024
+//            remain), then each thread rescans its K points from its prefix.
+//            ~2 + 2/16 additions per point, one
 //            point-addition site per kernel, no waits between blocks.  Correct
 //            for every length (the reference's kernel indexes its tile sums
 //            wrongly above 256 x grid points, ftcrypto.cu:1512).
@@ -86,12 +87,13 @@ __global__ void __launch_bounds__(NT) k_reduce(const uint4 *p, size_t s, size_t 
 
 // ------------------------------------------------------------ scan
 
-// inclusive scan over the warp; returns the lane's inclusive sum in acc
-FT_DEV void warp_scan_incl(ge_p3 &acc)
+// inclusive scan over the first `width` lanes of the warp (a power of two);
+// returns the lane's inclusive sum in acc
+FT_DEV void warp_scan_incl(ge_p3 &acc, int width = 32)
 {
     const int lane = threadIdx.x & 31;
 #pragma unroll 1
-    for (int o = 1; o < 32; o <<= 1) {
+    for (int o = 1; o < width; o <<= 1) {
         ge_p3 up, sum;
         shfl_up_p3(up, acc, o);
         sum = up;
@@ -104,6 +106,7 @@ FT_DEV void warp_scan_incl(ge_p3 &acc)
 template <int NT>
 FT_DEV void block_scan_excl(ge_p3 &ex, const ge_p3 &x, uint4 *sm /* (NT/32) * 8 */)
 {
+    static_assert(NT >= 64 && NT <= 1024 && (NT & (NT - 1)) == 0, "a power-of-two number of warps");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     ge_p3 incl = x;
     warp_scan_incl(incl);
@@ -113,7 +116,7 @@ FT_DEV void block_scan_excl(ge_p3 &ex, const ge_p3 &x, uint4 *sm /* (NT/32) * 8 
         ge_p3 w;
         if (lane < NT / 32) sm_ld_p3(w, sm, lane);
         else ge_p3_0(w);
-        warp_scan_incl(w);
+        warp_scan_incl(w, NT / 32); // the warps' totals: log2(NT/32) levels, not 5
         ge_p3 wex;
         shfl_up_p3(wex, w, 1);
         if (lane == 0) ge_p3_0(wex);
@@ -173,18 +176,22 @@ __global__ void __launch_bounds__(128) k_scan_apply(uint4 *p, size_t s, size_t n
     }
 }
 
-// one block scans n <= NT * K points in place: thread sums, a block-wide
-// exclusive scan of them, then the sequential rescan
-template <int NT, int K>
-__global__ void __launch_bounds__(NT) k_scan_small(uint4 *p, size_t s, size_t n, int exclusive)
+// one block scans n <= NT * kpt points in place: sums of kpt consecutive
+// points per thread, a block-wide exclusive scan of them, then the
+// sequential rescan.  One block is latency-bound, so the points are spread
+// over all NT threads (kpt = ceil(n / NT)): the last level of a 4M-point scan
+// (1,024 points) is a chain of 17 dependent additions instead of 41 with a
+// fixed 16 points per thread (194 us per launch).
+template <int NT>
+__global__ void __launch_bounds__(NT) k_scan_small(uint4 *p, size_t s, size_t n, int kpt, int exclusive)
 {
     __shared__ uint4 sm[(NT / 32) * 8];
-    const size_t e0 = (size_t)threadIdx.x * K;
+    const size_t e0 = (size_t)threadIdx.x * kpt;
     ge_p3 acc;
     ge_p3_0(acc);
     if (e0 < n) ld_p3(acc, p, s, e0);
 #pragma unroll 1
-    for (int k = 1; k < K; ++k) {
+    for (int k = 1; k < kpt; ++k) {
         const size_t e = e0 + k;
         if (e >= n) break;
         ge_p3 x;
@@ -194,7 +201,7 @@ __global__ void __launch_bounds__(NT) k_scan_small(uint4 *p, size_t s, size_t n,
     ge_p3 pre;
     block_scan_excl<NT>(pre, acc, sm);
 #pragma unroll 1
-    for (int k = 0; k < K; ++k) {
+    for (int k = 0; k < kpt; ++k) {
         const size_t e = e0 + k;
         if (e >= n) break;
         ge_p3 x;
@@ -209,25 +216,32 @@ static const int SMALL_NT = 256;
 
 size_t scan_scratch_bytes(size_t n) { return scan_scratch_points(n) * 128 + 256; }
 
-// thread sums of SCAN_K points, an exclusive scan of those sums (the same
-// routine on an array SCAN_K times shorter, until one block suffices), then
-// the rescan: about 2 + 2/SCAN_K additions per point, no waits between blocks
+// thread sums of K = scan_level_k(n) points, an exclusive scan of those sums
+// (the same routine on an array K times shorter, until one block suffices),
+// then the rescan: about 2 + 2/K additions per point, no waits between blocks.
+// At 4M points the lower levels (262,144 points down to 4,096) take 4 points
+// per thread: 16 made each of their launches a 16-addition chain in
+// under-filled waves (~60 us each).
 cudaError_t scan(View v, size_t n, int exclusive, void *scratch, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
     if (n <= SCAN_SMALL_MAX) {
-        k_scan_small<SMALL_NT, SCAN_SMALL_MAX / SMALL_NT><<<1, SMALL_NT, 0, st>>>(v.p, v.s, n, exclusive);
+        const int kpt = (int)((n + SMALL_NT - 1) / SMALL_NT);
+        k_scan_small<SMALL_NT><<<1, SMALL_NT, 0, st>>>(v.p, v.s, n, kpt, exclusive);
         return cudaGetLastError();
     }
-    const size_t nt = (n + SCAN_K - 1) / SCAN_K;
+    const size_t K = scan_level_k(n);
+    const size_t nt = (n + K - 1) / K;
     View ts{(uint4 *)scratch, nt};
     void *rest = ts.p + FT_PLANES * nt;
     const unsigned grid = (unsigned)((nt + 127) / 128);
-    k_scan_sums<SCAN_K><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s);
+    if (K == 16) k_scan_sums<16><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s);
+    else k_scan_sums<4><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if ((e = scan(ts, nt, 1, rest, st)) != cudaSuccess) return e;
-    k_scan_apply<SCAN_K><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s, exclusive);
+    if (K == 16) k_scan_apply<16><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s, exclusive);
+    else k_scan_apply<4><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s, exclusive);
     return cudaGetLastError();
 }
 

@@ -334,6 +334,21 @@ def test_reduce_scan_prescan(ft, orc, n):
     assert (X.to_bytes_folded() == orc.encode(orc.scan(a, exclusive=True))).all()
 
 
+@pytest.mark.parametrize("n", [262145, 300001])
+def test_scan_large_by_linearity(ft, n):
+    # sizes whose top level takes 16 points per thread: the scan of k_i * B
+    # is (k_0 + ... + k_i) * B, computed by the comb from the prefix sums
+    g = synth.rng(300 + n)
+    k = g.integers(0, 1 << 20, n).astype(np.uint64)
+    S = ft.Array.from_small_scalars(k)
+    S.scan()
+    assert (S.to_bytes_folded() == ft.Array.from_small_scalars(np.cumsum(k)).to_bytes_folded()).all()
+    X = ft.Array.from_small_scalars(k)
+    X.prescan()
+    ex = np.concatenate([[0], np.cumsum(k)[:-1]]).astype(np.uint64)
+    assert (X.to_bytes_folded() == ft.Array.from_small_scalars(ex).to_bytes_folded()).all()
+
+
 @pytest.mark.parametrize("n,nseg", [(1, 1), (10, 10), (100, 1), (1000, 63), (20000, 1250), (70000, 2000)])
 def test_segmented_sum_csr(ft, orc, n, nseg):
     g = synth.rng(300 + n)
