@@ -265,11 +265,11 @@ def e2e(args, dist, ft, torch, state):
     import ctypes
     pk, m, r, k = state
     L = ft.api.lib()
-    hm = torch.from_numpy(to_i64(m)).pin_memory().numpy().view(np.uint64)
-    hr = torch.from_numpy(r).pin_memory().numpy()
-    hk = torch.from_numpy(k).pin_memory().numpy()
-    out1 = torch.empty(N_CT * 160, dtype=torch.uint8).pin_memory().numpy()
-    out2 = torch.empty(N_CT * 160, dtype=torch.uint8).pin_memory().numpy()
+    hm_t, hr_t, hk_t = (torch.from_numpy(x).pin_memory() for x in (to_i64(m), r, k))
+    o1_t, o2_t = (torch.empty(N_CT * 160, dtype=torch.uint8).pin_memory() for _ in range(2))
+    hm = hm_t.numpy().view(np.uint64)
+    hr, hk = hr_t.numpy(), hk_t.numpy()
+    out1, out2 = o1_t.numpy(), o2_t.numpy()
     p1 = out1.ctypes.data_as(ctypes.c_void_p)
     p2 = out2.ctypes.data_as(ctypes.c_void_p)
 
@@ -291,9 +291,47 @@ def e2e(args, dist, ft, torch, state):
         step()
     sec = time.perf_counter() - t
     sec_max = dist.max(sec)
+    h2d_ms, d2h_ms = copy_times(torch, (hm_t, hr_t, hk_t, hk_t), (o1_t, o2_t))
     return {"value": dist.ws * args.steps * N_CT * SMUL_PER_CT / sec_max, "unit": UNIT,
             "h2d_bytes_per_step": int(hm.nbytes + hr.nbytes + 2 * hk.nbytes),
-            "d2h_bytes_per_step": int(out1.nbytes + out2.nbytes), "ms_per_step": sec_max / args.steps * 1e3}
+            "d2h_bytes_per_step": int(out1.nbytes + out2.nbytes), "ms_per_step": sec_max / args.steps * 1e3,
+            "h2d_ms_alone": h2d_ms, "d2h_ms_alone": d2h_ms}
+
+
+def copy_times(torch, ins, outs, reps=5):
+    """The step's host<->device bytes timed alone as plain copies between the
+    same pinned buffers and device memory (CUDA events, median of reps): the
+    part of the e2e step that the host link sets."""
+    dev_in = torch.empty(sum(t.numel() * t.element_size() for t in ins), dtype=torch.uint8, device="cuda")
+    dev_out = torch.empty(outs[0].numel(), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+
+    def h2d():
+        off = 0
+        for t in ins:
+            b = t.view(torch.uint8).reshape(-1)
+            dev_in[off:off + b.numel()].copy_(b, non_blocking=True)
+            off += b.numel()
+
+    def d2h():
+        for t in outs:
+            t.copy_(dev_out[:t.numel()], non_blocking=True)
+
+    res = []
+    for fn in (h2d, d2h):
+        ts = []
+        with torch.cuda.stream(s):
+            fn()
+            for _ in range(reps):
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(s)
+                fn()
+                b.record(s)
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+        res.append(statistics.median(ts))
+    return res
 
 
 # ---------------------------------------------------------------- secondary
@@ -622,6 +660,7 @@ def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slot
 # ---------------------------------------------------------------- CPU side
 
 CPU_SAMPLE_CT = 65536
+CPU_SAMPLE_1T = 2048
 
 
 def cpu_run(n_ct: int, threads: int, seed: int):
@@ -643,13 +682,39 @@ def cpu_run(n_ct: int, threads: int, seed: int):
     return time.perf_counter() - t
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (x86) or implementer/part ids (Arm)."""
+    import platform
+    fields = {}
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if ":" in line:
+                    key, val = (x.strip() for x in line.split(":", 1))
+                    fields.setdefault(key, val)
+    except OSError:
+        pass
+    if "model name" in fields:
+        return fields["model name"]
+    if "CPU part" in fields:
+        known = {("0x41", "0xd4f"): "Arm Neoverse V2"}
+        key = (fields.get("CPU implementer", "?"), fields["CPU part"])
+        name = known.get(key, f"CPU implementer {key[0]}, part {key[1]}")
+        return f"{platform.machine()} ({name})"
+    return platform.machine()
+
+
 def cpu_baseline():
     cores = os.cpu_count() or 1
     sec = cpu_run(CPU_SAMPLE_CT, cores, SEED)
+    sec1 = cpu_run(CPU_SAMPLE_1T, 1, SEED + 1)
     return {"value": CPU_SAMPLE_CT * SMUL_PER_CT / sec, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{CPU_SAMPLE_CT} ciphertexts of the same workload (encrypt as 3 variable-base "
                       f"products + add, then 2 products), oracle restatement of the reference "
-                      f"arithmetic, {cores} threads, {sec:.2f} s"}
+                      f"arithmetic, {cores} threads, {sec:.2f} s",
+            "single_thread_value": CPU_SAMPLE_1T * SMUL_PER_CT / sec1,
+            "single_thread_sample": f"{CPU_SAMPLE_1T} ciphertexts on 1 thread, {sec1:.2f} s",
+            "cpu_model": cpu_model()}
 
 
 def run_reference(args):
@@ -675,7 +740,8 @@ def run_reference(args):
                              "sample": f"{n} ciphertexts per step on {cores} host threads: the oracle's "
                                        "restatement of the reference arithmetic (sodium_fe.cu/sodium_ge.cu) "
                                        "in the reference's composition; the reference's own build is "
-                                       "x86-only here and its sources are absent on the GPU host"},
+                                       "x86-only here and its sources are absent on the GPU host",
+                             "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
