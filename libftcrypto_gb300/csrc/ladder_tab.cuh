@@ -114,9 +114,9 @@ struct HybridTab {
             fe_cmov(f, e, ct_eq_mask(babs, (uint32_t)(k + 1)));
         }
         if (NE <= 4) return;
-        // (a select split over the logic and multiply-add pipes, as in the
-        // encryption kernel, measured 3% slower here: the field
-        // multiplications keep the multiply-add pipe busy)
+        // (a select with some entries multiplied by 0/1 indicators on the
+        // multiply-add pipe instead of masked measured 3% slower: the field
+        // multiplications keep that pipe busy)
         uint32_t r[32];
         tmem_ld32(col + 32u * (uint32_t)j, r);
 #pragma unroll

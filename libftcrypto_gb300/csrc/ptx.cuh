@@ -23,12 +23,3 @@ FT_DEV uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm
 FT_DEV uint32_t madc_hi(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm volatile("madc.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r; }
 FT_DEV uint32_t mul_lo(uint32_t a, uint32_t b) { return a * b; }
 FT_DEV uint32_t mul_hi(uint32_t a, uint32_t b) { return __umulhi(a, b); }
-// a * b + c on the multiply-add pipe: constant-time selects multiply table
-// words by 0/1 indicators with it to move work off the logic pipe (the asm
-// keeps the product from being rewritten as a select)
-FT_DEV uint32_t imad_u32(uint32_t a, uint32_t b, uint32_t c)
-{
-    uint32_t r;
-    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
-    return r;
-}
