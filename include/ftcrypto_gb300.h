@@ -117,8 +117,10 @@ ft_error ftx_scale_bounded(ft_ge25519_array array, uint32_t k, unsigned bits);
  * current contents).  Operations of one batch run concurrently: an array
  * written by one operation must not appear in any other operation of the
  * batch (FT_ERR_BAD_SIZE at record time otherwise).  Arrays must stay
- * allocated and keep their length while the batch exists; recording after
- * the first run returns FT_ERR_BAD_SIZE. */
+ * allocated and keep their storage while the batch exists: a run after
+ * ft_array_set_length, ft_array_reduce or ft_array_delete_* changed a
+ * recorded array returns FT_ERR_SIZE_MISMATCH and launches nothing.
+ * Recording after the first run returns FT_ERR_BAD_SIZE. */
 struct ftx_batch_s;
 typedef struct ftx_batch_s *ftx_batch;
 ft_error ftx_batch_create(ftx_batch *batch);

@@ -1143,6 +1143,14 @@ struct ftx_batch_s {
     std::vector<ft::BatchItem> items; // SEG items hold an index into offs in `off` until uploaded
     std::vector<int32_t> offs;
     std::set<const void *> written, read;
+    // every recorded array with the storage it had then: the work items hold
+    // raw device addresses, so a run refuses arrays that were reallocated
+    struct Rec {
+        const ft_ge25519_array_s *a;
+        const uint4 *planes;
+        size_t cap, n;
+    };
+    std::vector<Rec> arrays;
     size_t n_ops = 0;
     ft::BatchItem *d_items = nullptr;
     int32_t *d_offs = nullptr;
@@ -1166,6 +1174,8 @@ ft_error claim(ftx_batch b, const void *w, const void *r)
     b->n_ops++;
     return FT_ERR_NO_ERROR;
 }
+
+void note(ftx_batch b, const_ft_ge25519_array a) { b->arrays.push_back({a, a->planes, a->cap, a->n}); }
 
 // scales (longest ladders first), then segmented sums, then adds
 int item_rank(const ft::BatchItem &it)
@@ -1234,6 +1244,8 @@ ft_error ftx_batch_add(ftx_batch b, ft_ge25519_array res, const_ft_ge25519_array
     if (res->n != summand->n) return FT_ERR_SIZE_MISMATCH;
     ft_error err = claim(b, res->planes, summand->planes);
     if (err) return err;
+    note(b, res);
+    note(b, summand);
     const size_t per = (size_t)ft::batch_block() * g_batch_add_pts;
     for (size_t base = 0; base < res->n; base += per) {
         ft::BatchItem it{};
@@ -1253,6 +1265,7 @@ ft_error ftx_batch_scale_bounded(ftx_batch b, ft_ge25519_array a, uint32_t k, un
     if (bits < 1 || bits > 32 || (bits < 32 && (k >> bits))) return FT_ERR_BAD_SIZE;
     ft_error err = claim(b, a->planes, nullptr);
     if (err) return err;
+    note(b, a);
     const size_t per = (size_t)ft::batch_block();
     for (size_t base = 0; base < a->n; base += per) {
         ft::BatchItem it{};
@@ -1281,6 +1294,8 @@ ft_error ftx_batch_segmented_sum(ftx_batch b, ft_ge25519_array out, const int32_
         if (off[s + 1] < off[s]) return FT_ERR_BAD_SIZE;
     ft_error err = claim(b, out->planes, src->planes);
     if (err) return err;
+    note(b, out);
+    note(b, src);
     const size_t base_off = b->offs.size();
     b->offs.insert(b->offs.end(), off, off + nseg + 1);
     const size_t per = (size_t)ft::batch_block();
@@ -1301,6 +1316,8 @@ ft_error ftx_batch_segmented_sum(ftx_batch b, ft_ge25519_array out, const int32_
 ft_error ftx_batch_run(ftx_batch b)
 {
     ENSURE_INIT();
+    for (const auto &r : b->arrays)
+        if (r.a->planes != r.planes || r.a->cap != r.cap || r.a->n != r.n) return FT_ERR_SIZE_MISMATCH;
     if (!b->ready) {
         ft_error err = batch_upload(b);
         if (err) return err;

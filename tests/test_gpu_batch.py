@@ -197,3 +197,19 @@ def test_batch_rejects_conflicts(ft):
     b.run()
     with pytest.raises(ft.FtError):
         b.scale_small(ft.Array.from_scalars(synth.scalars_mod_L(g, 2)), 3)  # recorded after the first run
+
+
+def test_batch_refuses_reallocated_arrays(ft, orc):
+    g = synth.rng(34)
+    sa, sc = synth.scalars_mod_L(g, 40), synth.scalars_mod_L(g, 40)
+    a, c = ft.Array.from_scalars(sa), ft.Array.from_scalars(sc)
+    b = ft.Batch()
+    b.add(a, c)
+    b.run()
+    want = orc.encode(orc.add(orc.from_scalars(sa), orc.from_scalars(sc)))
+    assert (a.to_bytes_folded() == want).all()
+    a.set_length(10)  # at most half: new storage, which the work list does not know
+    with pytest.raises(ft.FtError) as e:
+        b.run()
+    assert e.value.code == 2
+    assert (a.to_bytes_folded() == want[:10]).all()  # nothing ran
