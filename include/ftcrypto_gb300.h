@@ -205,7 +205,7 @@ int ftx_tune_get(int knob);
  * counterpart in the reference: it exists for callers that cannot allocate
  * device memory (their memory is held by another allocator, or they must not
  * trigger cudaMalloc's synchronisation).  It allocates nothing; the scan's
- * scratch is a fixed array of about 9 MB that the library keeps on every
+ * scratch is a fixed array of about 11 MB that the library keeps on every
  * GPU that loads it.  n <= FT_NOALLOC_SCAN_MAX_POINTS (FT_ERR_BAD_SIZE
  * otherwise).  All calls share that array: calls that overlap on the GPU
  * race and must be serialised.  The first call on a device looks up the

@@ -11,7 +11,7 @@
 //
 // Limits and sharing:
 //  * at most FT_NOALLOC_SCAN_MAX_POINTS points per call (FT_ERR_BAD_SIZE
-//    beyond it); the array is FT_NOALLOC_SCAN_SCRATCH_BYTES (about 9 MB) and
+//    beyond it); the array is FT_NOALLOC_SCAN_SCRATCH_BYTES (about 11 MB) and
 //    is resident on every GPU that loads the library until the process exits;
 //  * every call uses the same array and leaves its partial sums there; each
 //    launch writes all scratch it later reads, so nothing must start at zero;
