@@ -32,9 +32,18 @@ struct Ctx {
     size_t scratch_cap = 0;
     long long *d_status = nullptr; // one device word for "last bad index"
     ft_error last_void = FT_ERR_NO_ERROR;
-    uint8_t pk_bytes[32];
-    uint32_t *pk_table = nullptr; // encryption tables of B and of the cached public key
-    bool pk_valid = false;
+    // encryption tables (B's and a public key's) of the last PK_CACHE keys
+    // used, least recently used replaced: a table costs ~0.55 ms to build
+    // (255 doublings in sequence for its last row), so callers alternating
+    // between a few keys build each once
+    struct KeyTab {
+        uint8_t pk[32];
+        uint32_t *table = nullptr;
+        uint64_t used = 0; // 0: empty
+    };
+    static constexpr int PK_CACHE = 4;
+    KeyTab keys[PK_CACHE];
+    uint64_t key_clock = 0;
     uint32_t *b_table = nullptr;  // radix-32 comb table of B (fixed-base products)
     void *dlog_mem = nullptr;     // decryption table of j*B, j < dlog.m_max
     ft::DlogTable dlog;
@@ -248,15 +257,27 @@ ft_error build_key_tables(uint32_t *d_tables, const uint8_t *pk)
     return FT_ERR_NO_ERROR;
 }
 
-ft_error ensure_pk_table(const uint8_t *pk)
+// the encryption tables of pk, from the cache or built into its least
+// recently used slot (kernels still queued on the library stream that read
+// the slot's old tables run before the rebuild, in stream order)
+ft_error ensure_pk_table(const uint8_t *pk, const uint32_t **tables)
 {
-    if (g.pk_valid && std::memcmp(g.pk_bytes, pk, 32) == 0) return FT_ERR_NO_ERROR;
-    g.pk_valid = false;
-    if (!g.pk_table) CK(dev_alloc((void **)&g.pk_table, ft::ENC_TABLES_BYTES));
-    ft_error err = build_key_tables(g.pk_table, pk);
+    Ctx::KeyTab *slot = &g.keys[0];
+    for (Ctx::KeyTab &k : g.keys) {
+        if (k.used && std::memcmp(k.pk, pk, 32) == 0) {
+            k.used = ++g.key_clock;
+            *tables = k.table;
+            return FT_ERR_NO_ERROR;
+        }
+        if (k.used < slot->used) slot = &k;
+    }
+    slot->used = 0;
+    if (!slot->table) CK(dev_alloc((void **)&slot->table, ft::ENC_TABLES_BYTES));
+    ft_error err = build_key_tables(slot->table, pk);
     if (err) return err;
-    std::memcpy(g.pk_bytes, pk, 32);
-    g.pk_valid = true;
+    std::memcpy(slot->pk, pk, 32);
+    slot->used = ++g.key_clock;
+    *tables = slot->table;
     return FT_ERR_NO_ERROR;
 }
 
@@ -901,9 +922,10 @@ ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint
     ENSURE_INIT();
     if (bits < 1 || bits > 64) return FT_ERR_BAD_SIZE;
     if (c1->n != n || c2->n != n) return FT_ERR_SIZE_MISMATCH;
-    ft_error err = ensure_pk_table(pk);
+    const uint32_t *tab;
+    ft_error err = ensure_pk_table(pk, &tab);
     if (err) return err;
-    CK(ft::encrypt(ft::view_of(c1), ft::view_of(c2), n, d_r, d_m, m_digits(bits), g.pk_table, g.stream));
+    CK(ft::encrypt(ft::view_of(c1), ft::view_of(c2), n, d_r, d_m, m_digits(bits), tab, g.stream));
     return FT_ERR_NO_ERROR;
 }
 
@@ -915,7 +937,8 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
     if (bits < 64)
         for (size_t i = 0; i < n; ++i)
             if (m[i] >> bits) return FT_ERR_BAD_SIZE;
-    ft_error err = ensure_pk_table(pk);
+    const uint32_t *tab;
+    ft_error err = ensure_pk_table(pk, &tab);
     if (err) return err;
     ft_ge25519_array a, b;
     if ((err = arr_new(&a, n))) return err;
@@ -930,7 +953,7 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
     if (e == cudaSuccess) e = h2d((uint8_t *)s + br, m, n * 8);
     if (e == cudaSuccess)
         e = ft::encrypt(ft::view_of(a), ft::view_of(b), n, (const uint8_t *)s, (const uint64_t *)((uint8_t *)s + br),
-                        m_digits(bits), g.pk_table, g.stream);
+                        m_digits(bits), tab, g.stream);
     if (e != cudaSuccess) {
         ft_array_free(a);
         ft_array_free(b);
@@ -973,9 +996,10 @@ ft_error ftx_rerandomise_device(ft_ge25519_array c1, ft_ge25519_array c2, const 
 {
     ENSURE_INIT();
     if (c1->n != n || c2->n != n) return FT_ERR_SIZE_MISMATCH;
-    ft_error err = ensure_pk_table(pk);
+    const uint32_t *tab;
+    ft_error err = ensure_pk_table(pk, &tab);
     if (err) return err;
-    CK(ft::rerandomise(ft::view_of(c1), ft::view_of(c2), n, d_r, g.pk_table, g.stream));
+    CK(ft::rerandomise(ft::view_of(c1), ft::view_of(c2), n, d_r, tab, g.stream));
     return FT_ERR_NO_ERROR;
 }
 
@@ -983,13 +1007,14 @@ ft_error ftx_rerandomise(ft_ge25519_array c1, ft_ge25519_array c2, const uint8_t
 {
     ENSURE_INIT();
     if (c1->n != n || c2->n != n) return FT_ERR_SIZE_MISMATCH;
-    ft_error err = ensure_pk_table(pk);
+    const uint32_t *tab;
+    ft_error err = ensure_pk_table(pk, &tab);
     if (err) return err;
     if (n == 0) return FT_ERR_NO_ERROR;
     void *s;
     CK(scratch(&s, align256(n * 32)));
     CK(h2d(s, r, n * 32));
-    CK(ft::rerandomise(ft::view_of(c1), ft::view_of(c2), n, (const uint8_t *)s, g.pk_table, g.stream));
+    CK(ft::rerandomise(ft::view_of(c1), ft::view_of(c2), n, (const uint8_t *)s, tab, g.stream));
     return FT_ERR_NO_ERROR;
 }
 

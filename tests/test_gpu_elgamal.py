@@ -135,3 +135,20 @@ def test_ct_add_sub_match_ft_add(ft, orc, n):
         with pytest.raises(ft.FtError) as e:
             ft.ct_add(c1, c2, d1.get_range(0, n - 1, 1) if n > 1 else ft.Array.init_scalar(2), d2)
         assert e.value.code == 2
+
+
+def test_encrypt_with_alternating_keys(ft, orc):
+    # more keys than the library caches key tables for, used in turn and
+    # again: each encryption equals the oracle's under its own key
+    g = synth.rng(77)
+    ks = [synth.scalars_mod_L(g, 1) for _ in range(6)]
+    pks = [orc.encode(orc.from_scalars(sk))[0] for sk in ks]
+    n = 33
+    for rnd in range(2):
+        for j in (0, 1, 2, 3, 4, 5, 1, 0):
+            m = synth.plaintexts(g, n, 255)
+            r = synth.scalars_mod_L(g, n)
+            c1, c2 = ft.encrypt(pks[j], m, r, 8)
+            o1, o2 = orc.encrypt(pks[j], m, r)
+            assert (c1.to_bytes_folded() == orc.encode(o1)).all()
+            assert (c2.to_bytes_folded() == orc.encode(o2)).all(), (rnd, j)
