@@ -298,7 +298,7 @@ def e2e(args, dist, ft, torch, state):
             "h2d_ms_alone": h2d_ms, "d2h_ms_alone": d2h_ms}
 
 
-def copy_times(torch, ins, outs, reps=5):
+def copy_times(torch, ins, outs, reps=11):
     """The step's host<->device bytes timed alone as plain copies between the
     same pinned buffers and device memory (CUDA events, median of reps): the
     part of the e2e step that the host link sets."""
@@ -398,7 +398,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     s1, s2 = a1.get_range(0, n1, 1), a2.get_range(0, n1, 1)
     ft.ct_add(s1, s2, b1, b2)
     ok = decrypt_matches(ft, s1, s2, sk[0], ma + mb)
-    ms = timed(ev, lambda: ft.ct_add(a1, a2, b1, b2), 9, flush)
+    ms = timed(ev, lambda: ft.ct_add(a1, a2, b1, b2), 11, flush)
     out["ct_add_65536"] = {"ct_adds_per_s": n1 / (ms * 1e-3), "ms": ms, "decrypt_check": ok, "l2": "flushed",
                            **roof(2 * n1 * 3 * B_PT, 2 * n1 * W_ALG_PTADD, ms, hbm_peak, imad)}
 
@@ -410,7 +410,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     c1.reduce_into(r1, 0)
     c2.reduce_into(r2, 0)
     ok = decrypt_matches(ft, r1, r2, sk[0], [int(m3.sum())])
-    ms = timed(ev, lambda: (c1.reduce_into(r1, 0), c2.reduce_into(r2, 0)), 3)
+    ms = timed(ev, lambda: (c1.reduce_into(r1, 0), c2.reduce_into(r2, 0)), 11)
     out["reduce_16M_ct"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok,
                             **roof(2 * n3 * B_PT, 2 * n3 * W_ALG_PTADD, ms, hbm_peak, imad)}
 
@@ -425,7 +425,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     segm = np.add.reduceat(m3, off[:-1]).astype(np.uint64)
     ok = decrypt_matches(ft, o1, o2, sk[0], segm)
     ms = timed(ev, lambda: (ft.segmented_sum_csr_device(o1, d_off.data_ptr(), nseg, c1),
-                            ft.segmented_sum_csr_device(o2, d_off.data_ptr(), nseg, c2)), 3)
+                            ft.segmented_sum_csr_device(o2, d_off.data_ptr(), nseg, c2)), 11)
     seg_bytes = 2 * (n3 * B_PT + nseg * B_PT) + (nseg + 1) * 4
     out["segsum_16M_ct_1M_seg"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok,
                                    **roof(seg_bytes, 2 * (n3 - nseg) * W_ALG_PTADD, ms, hbm_peak, imad)}
@@ -440,7 +440,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     t2.scan()
     idx = np.sort(g.choice(n4, 64, replace=False))
     ok = decrypt_matches(ft, t1.get_subset(idx), t2.get_subset(idx), sk[0], np.cumsum(m4)[idx])
-    ms = timed(ev, lambda: (t1.scan(), t2.scan()), 3)
+    ms = timed(ev, lambda: (t1.scan(), t2.scan()), 11)
     out["scan_4M_ct"] = {"ct_per_s": n4 / (ms * 1e-3), "ms": ms, "decrypt_check_sample": ok,
                          **roof(2 * n4 * 2 * B_PT, 2 * n4 * W_ALG_PTADD, ms, hbm_peak, imad)}
     del c1, c2, t1, t2
@@ -449,7 +449,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     return out
 
 
-def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=3):
+def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=5):
     """4,096 ciphertext arrays, lengths log-uniform in [1, 65,536], each with
     one op (add 40%, scale by k in [1,1000] 30%, segmented sum of mean-8
     segments 30%): one persistent launch replayed from a CUDA graph against
