@@ -1179,7 +1179,7 @@ struct ftx_batch_s {
     size_t n_ops = 0;
     ft::BatchItem *d_items = nullptr;
     int32_t *d_offs = nullptr;
-    int *d_counter = nullptr;
+    unsigned *d_counter = nullptr;
     cudaGraphExec_t exec = nullptr;
     int w = 4; // window width of the scale items, fixed at upload
     bool ready = false;

@@ -157,7 +157,7 @@ int batch_block();
 size_t batch_smem_bytes();
 // w: window width 2..4 of the scale items
 cudaError_t batch_prepare(int w); // once, outside any stream capture
-cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, int w, cudaStream_t st);
+cudaError_t batch_launch(const BatchItem *d_items, int nitems, unsigned *d_counter, int w, cudaStream_t st);
 // v[i] = k * v[i] in nwin constant-time windows (k < 2^bits, nwin for bits)
 cudaError_t scale_small(View v, size_t n, uint32_t k, int nwin, int w, cudaStream_t st);
 

@@ -3,9 +3,12 @@
 //
 // k_batch: one block per SM (384 threads: the ladder tables of the scale
 //   path fill the SM's shared memory and half of its tensor memory, as in
-//   k_smul_var_tm) loops pulling work items from an atomic counter until the
-//   list is exhausted.  Items are pre-sorted costliest first, so the tail of
-//   the run is short ones (longest-processing-time order).  Item kinds:
+//   k_smul_var_tm).  Each warp loops pulling a 32-thread slice of a work item
+//   (item i, slice j: the item's logical threads 32j..32j+31) from an atomic
+//   counter until the list is exhausted, so a warp that finishes its slice
+//   early takes the next one instead of waiting at a block barrier for the
+//   item's slowest warp.  Items are pre-sorted costliest first, so the tail
+//   of the run is short ones (longest-processing-time order).  Item kinds:
 //     ADD    dst[i] += src[i] for count points (count <= 384 x points/thread)
 //     SCALE  dst[i] = k * dst[i], count <= 384 points, one per thread,
 //            constant time in k < 2^bits (smul_ladder_u32 in nwin windows
@@ -45,27 +48,30 @@ FT_DEV void scale_small_lane(uint4 *p, size_t s, size_t i, bool live, uint32_t k
     if (live) st_p3(p, s, i, h);
 }
 
+static constexpr int BATCH_WARPS = BATCH_NT / 32; // slices of an item
+
 template <int W>
 __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
-    k_batch(const BatchItem *items, int nitems, int *counter)
+    k_batch(const BatchItem *items, int nitems, unsigned *counter)
 {
     extern __shared__ uint4 smem[];
-    __shared__ int s_item;
     __shared__ uint32_t s_taddr;
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) tmem_alloc(&s_taddr, 512u);
     tmem_sync_threads();
     const HybridTab<BATCH_NT> tab{smem + tid, tmem_warp_addr(s_taddr, warp, 128u * (uint32_t)(warp >> 2))};
+    const unsigned nslices = (unsigned)nitems * BATCH_WARPS; // < 2^31 (checked at launch)
     for (;;) {
-        if (tid == 0) s_item = atomicAdd(counter, 1);
-        __syncthreads();
-        const int it = s_item;
-        __syncthreads();
-        if (it >= nitems) break;
+        unsigned sl = 0;
+        if (lane == 0) sl = atomicAdd(counter, 1u);
+        sl = __shfl_sync(0xffffffffu, sl, 0);
+        if (sl >= nslices) break;
+        const int it = (int)(sl / BATCH_WARPS);
+        const uint32_t tt = (sl % BATCH_WARPS) * 32u + (uint32_t)lane; // logical thread of the item
         const BatchItem w = items[it];
         if (w.op == BATCH_ADD) {
 #pragma unroll 1
-            for (uint32_t e = tid; e < w.count; e += BATCH_NT) {
+            for (uint32_t e = tt; e < w.count; e += BATCH_NT) {
                 ge_p3 x, y;
                 ld_p3(x, w.dst, w.dst_s, e);
                 ld_p3(y, w.src, w.src_s, e);
@@ -73,11 +79,11 @@ __global__ void __maxnreg__(tm_max_regs<BATCH_NT>())
                 st_p3(w.dst, w.dst_s, e, x);
             }
         } else if (w.op == BATCH_SCALE) {
-            if ((uint32_t)(warp * 32) < w.count) // warp-uniform
-                scale_small_lane<W>(w.dst, w.dst_s, tid, (uint32_t)tid < w.count, w.k, (int)w.nwin, tab);
+            if (tt - (uint32_t)lane < w.count) // warp-uniform
+                scale_small_lane<W>(w.dst, w.dst_s, tt, tt < w.count, w.k, (int)w.nwin, tab);
         } else { // BATCH_SEG
 #pragma unroll 1
-            for (uint32_t sg = tid; sg < w.count; sg += BATCH_NT) {
+            for (uint32_t sg = tt; sg < w.count; sg += BATCH_NT) {
                 const int32_t a = w.off[sg], b = w.off[sg + 1];
                 ge_p3 acc;
                 ge_p3_0(acc);
@@ -132,11 +138,12 @@ cudaError_t batch_prepare(int w)
     return ensure_smem_attr(g_batch_attr[w - 2], k_batch_fn[w - 2], batch_smem_bytes());
 }
 
-cudaError_t batch_launch(const BatchItem *d_items, int nitems, int *d_counter, int w, cudaStream_t st)
+cudaError_t batch_launch(const BatchItem *d_items, int nitems, unsigned *d_counter, int w, cudaStream_t st)
 {
+    if (nitems < 0 || (long long)nitems * BATCH_WARPS >= (1ll << 31)) return cudaErrorInvalidValue;
     cudaError_t e = batch_prepare(w);
     if (e != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(d_counter, 0, sizeof(int), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
     const unsigned g = (unsigned)sm_count();
     const size_t sm = batch_smem_bytes();
     if (w == 2) k_batch<2><<<g, BATCH_NT, sm, st>>>(d_items, nitems, d_counter);
