@@ -50,7 +50,8 @@ __global__ void __launch_bounds__(NT, 1) k_smul_var(uint4 *p, size_t s, size_t n
 // per SM, so the 512-column allocation below never waits for another
 // block's.  Threads past n run the ladder on the identity with a zero scalar
 // and store nothing, so every warp executes the warp-wide TMEM instructions
-// converged; no thread leaves before the final barrier and the free.
+// converged and every thread reaches the ladder's per-window barriers; no
+// thread leaves before the final barrier and the free.
 // Registers per thread the launch allows: the register file is four
 // 16,384-register partitions, one per warp scheduler, and the block's warps
 // are spread over them, so the busiest partition holds ceil(warps / 4) warps
@@ -84,7 +85,7 @@ __global__ void __maxnreg__(tm_max_regs<NT>()) k_smul_var_tm(uint4 *p, size_t s,
     __syncwarp();
     smul_build_table(tab, P);
     tmem_wait_st();
-    smul_ladder(h, a, tab);
+    smul_ladder(h, a, tab, true); // every thread runs the whole ladder
     if (live) st_p3(p, s, i, h);
     tmem_sync_threads();
     if (warp == 0) tmem_free(s_taddr, 512u);
