@@ -195,6 +195,15 @@ ft_error with_new_array(ft_ge25519_array *out, size_t n, F fill)
     return FT_ERR_NO_ERROR;
 }
 
+// the OR of n words: a branch-free loop the compiler vectorises (an
+// early-exit scan of 1,048,576 plaintexts cost more than its copy)
+uint64_t or_all(const uint64_t *v, size_t n)
+{
+    uint64_t acc = 0;
+    for (size_t i = 0; i < n; ++i) acc |= v[i];
+    return acc;
+}
+
 ft_error check_idxs(const size_t *idxs, size_t n, size_t bound)
 {
     for (size_t i = 0; i < n; ++i)
@@ -934,9 +943,7 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
 {
     ENSURE_INIT();
     if (bits < 1 || bits > 64) return FT_ERR_BAD_SIZE;
-    if (bits < 64)
-        for (size_t i = 0; i < n; ++i)
-            if (m[i] >> bits) return FT_ERR_BAD_SIZE;
+    if (bits < 64 && (or_all(m, n) >> bits)) return FT_ERR_BAD_SIZE;
     const uint32_t *tab;
     ft_error err = ensure_pk_table(pk, &tab);
     if (err) return err;

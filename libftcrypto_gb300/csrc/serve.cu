@@ -363,9 +363,11 @@ ft_error ftx_server_submit(ftx_server s, const ftx_request *req, uint64_t *ticke
     if (r.op < FTX_REQ_ENCRYPT || r.op > FTX_REQ_SEGSUM) return FT_ERR_BAD_SIZE;
     if (r.op == FTX_REQ_ENCRYPT) {
         if (r.plaintext_bits < 1 || r.plaintext_bits > 64) return FT_ERR_BAD_SIZE;
-        if (r.m && r.plaintext_bits < 64) // the comb reads only the digits of the bound
-            for (size_t i = 0; i < r.n; ++i)
-                if (r.m[i] >> r.plaintext_bits) return FT_ERR_BAD_SIZE;
+        if (r.m && r.plaintext_bits < 64) { // the comb reads only the digits of the bound
+            uint64_t acc = 0;
+            for (size_t i = 0; i < r.n; ++i) acc |= r.m[i];
+            if (acc >> r.plaintext_bits) return FT_ERR_BAD_SIZE;
+        }
     }
     if (r.op != FTX_REQ_ENCRYPT && (!r.c1 || !r.c2 || r.c1->n != r.n || r.c2->n != r.n)) return FT_ERR_SIZE_MISMATCH;
     if (r.op == FTX_REQ_SEGSUM) {
