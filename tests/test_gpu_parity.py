@@ -205,9 +205,8 @@ def test_fixed_base_edge_scalars(ft, orc):
 
 
 def test_export_into_pinned_memory(ft, orc):
-    """Exports into pinned (mapped) host memory, written by the conversion
-    kernels directly, equal the exports into pageable memory; an unaligned
-    pinned buffer takes the copying path."""
+    """Exports into pinned host memory, at an aligned and an unaligned
+    address, equal the exports into pageable memory."""
     torch = pytest.importorskip("torch")
     import ctypes
     g = synth.rng(13)
@@ -224,6 +223,28 @@ def test_export_into_pinned_memory(ft, orc):
             got = pin.numpy()[off:off + n * width]
             assert (got == want).all(), (width, off)
     assert (want.reshape(n, 64)[:, :32] != 0).any()
+
+
+def test_large_exports_equal_concatenated_ranges(ft):
+    """An export of 600,001 points equals the concatenated exports of three
+    sub-ranges (taken by get_range), in every format."""
+    import ctypes
+    g = synth.rng(14)
+    n = 600_001
+    a = ft.Array.from_small_scalars(g.integers(0, 1 << 40, n).astype(np.uint64))
+    L = ft.api.lib()
+    cuts = [0, 200_000, 400_000, n]
+    parts = [a.get_range(lo, hi, 1) for lo, hi in zip(cuts, cuts[1:])]
+    for fn, width in ((L.ft_array_to_bytes, 160), (L.ft_array_to_bytes_folded, 32), (L.ft_array_to_bytes_affine, 64),
+                      (L.ftx_array_to_packed, 128)):
+        got = np.zeros(n * width, np.uint8)
+        ft.check(fn(got.ctypes.data_as(ctypes.c_void_p), got.size, a.handle))
+        want = []
+        for p in parts:
+            w = np.zeros(len(p) * width, np.uint8)
+            ft.check(fn(w.ctypes.data_as(ctypes.c_void_p), w.size, p.handle))
+            want.append(w)
+        assert (got == np.concatenate(want)).all(), width
 
 
 def test_constructors(ft, orc):
