@@ -344,6 +344,57 @@ const char *ft_error_str(ft_error err)
     return errors[err];
 }
 
+} // extern "C"
+
+namespace {
+
+// the library's stream, memory pool, status word and B's comb table
+ft_error init_device(int dev)
+{
+    CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    cudaMemPoolProps pp;
+    std::memset(&pp, 0, sizeof pp);
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.handleTypes = cudaMemHandleTypeNone;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = dev;
+    CK(cudaMemPoolCreate(&g.pool, &pp));
+    uint64_t thr = UINT64_MAX;
+    CK(cudaMemPoolSetAttribute(g.pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    g.device = dev;
+    CK(cudaMallocFromPoolAsync((void **)&g.d_status, 256, g.pool, g.stream));
+    // the comb table of B, from B's encoding (y = 4/5, x even)
+    uint8_t benc[32];
+    std::memset(benc, 0x66, 32);
+    benc[0] = 0x58;
+    void *s;
+    CK(dev_alloc((void **)&g.b_table, ft::ENC_TABLE_WORDS * 4));
+    CK(dev_alloc(&s, align256(FT_PLANES_BYTES_PER_POINT) + 256));
+    ft::View bp{(uint4 *)s, 1};
+    uint8_t *d_enc = (uint8_t *)s + align256(FT_PLANES_BYTES_PER_POINT);
+    CK(cudaMemcpyAsync(d_enc, benc, 32, cudaMemcpyHostToDevice, g.stream));
+    CK(ft::decode(bp, d_enc, 1, g.d_status, g.stream));
+    CK(ft::build_enc_table(g.b_table, bp, g.stream));
+    CK(cudaStreamSynchronize(g.stream)); // benc is on the stack
+    dev_free(s);
+    CK(cudaStreamSynchronize(g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
+// undo a failed init_device, so that a later ft_crypto_init starts afresh
+void init_release()
+{
+    if (g.stream) cudaStreamSynchronize(g.stream);
+    if (g.pool) cudaMemPoolDestroy(g.pool); // releases its memory once nothing is outstanding
+    if (g.stream) cudaStreamDestroy(g.stream);
+    cudaGetLastError();
+    g = Ctx{};
+}
+
+} // namespace
+
+extern "C" {
+
 ft_error ft_crypto_init(void)
 {
     std::lock_guard<std::mutex> lk(g_init_mu);
@@ -360,35 +411,11 @@ ft_error ft_crypto_init(void)
     }
     // kernels are built for sm_103a only
     if (prop.major != 10 || prop.minor != 3) return FT_ERR_INSUFFICIENT_DEVICE_OR_DRIVER;
-    CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
-    cudaMemPoolProps pp;
-    std::memset(&pp, 0, sizeof pp);
-    pp.allocType = cudaMemAllocationTypePinned;
-    pp.handleTypes = cudaMemHandleTypeNone;
-    pp.location.type = cudaMemLocationTypeDevice;
-    pp.location.id = dev;
-    CK(cudaMemPoolCreate(&g.pool, &pp));
-    uint64_t thr = UINT64_MAX;
-    CK(cudaMemPoolSetAttribute(g.pool, cudaMemPoolAttrReleaseThreshold, &thr));
-    g.device = dev;
-    CK(cudaMallocFromPoolAsync((void **)&g.d_status, 256, g.pool, g.stream));
-    // the comb table of B, from B's encoding (y = 4/5, x even)
-    {
-        uint8_t benc[32];
-        std::memset(benc, 0x66, 32);
-        benc[0] = 0x58;
-        void *s;
-        CK(dev_alloc((void **)&g.b_table, ft::ENC_TABLE_WORDS * 4));
-        CK(dev_alloc(&s, align256(FT_PLANES_BYTES_PER_POINT) + 256));
-        ft::View bp{(uint4 *)s, 1};
-        uint8_t *d_enc = (uint8_t *)s + align256(FT_PLANES_BYTES_PER_POINT);
-        CK(cudaMemcpyAsync(d_enc, benc, 32, cudaMemcpyHostToDevice, g.stream));
-        CK(ft::decode(bp, d_enc, 1, g.d_status, g.stream));
-        CK(ft::build_enc_table(g.b_table, bp, g.stream));
-        CK(cudaStreamSynchronize(g.stream)); // benc is on the stack
-        dev_free(s);
+    ft_error err = init_device(dev);
+    if (err) {
+        init_release();
+        return err;
     }
-    CK(cudaStreamSynchronize(g.stream));
     g.inited = true;
     return FT_ERR_NO_ERROR;
 }
