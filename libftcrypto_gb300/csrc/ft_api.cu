@@ -970,24 +970,31 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
 {
     ENSURE_INIT();
     if (bits < 1 || bits > 64) return FT_ERR_BAD_SIZE;
-    if (bits < 64 && (or_all(m, n) >> bits)) return FT_ERR_BAD_SIZE;
+    if (too_long(n)) return FT_ERR_OUT_OF_MEMORY;
+    // the key's tables first (building them uses the scratch buffer)
     const uint32_t *tab;
     ft_error err = ensure_pk_table(pk, &tab);
     if (err) return err;
+    // both inputs are queued, the plaintext bound is checked on the host
+    // while pinned inputs are in flight, and one wait covers both
+    void *s;
+    size_t br = align256(n * 32);
+    CK(scratch(&s, br + align256(n * 8)));
+    if (n) {
+        CK(cudaMemcpyAsync(s, r, n * 32, cudaMemcpyHostToDevice, g.stream));
+        CK(cudaMemcpyAsync((uint8_t *)s + br, m, n * 8, cudaMemcpyHostToDevice, g.stream));
+    }
+    const bool bad = bits < 64 && (or_all(m, n) >> bits);
+    if (n && (host_is_pinned(r) || host_is_pinned(m))) CK(cudaStreamSynchronize(g.stream));
+    if (bad) return FT_ERR_BAD_SIZE;
     ft_ge25519_array a, b;
     if ((err = arr_new(&a, n))) return err;
     if ((err = arr_new(&b, n))) {
         ft_array_free(a);
         return err;
     }
-    void *s;
-    size_t br = align256(n * 32);
-    cudaError_t e = scratch(&s, br + align256(n * 8));
-    if (e == cudaSuccess) e = h2d(s, r, n * 32);
-    if (e == cudaSuccess) e = h2d((uint8_t *)s + br, m, n * 8);
-    if (e == cudaSuccess)
-        e = ft::encrypt(ft::view_of(a), ft::view_of(b), n, (const uint8_t *)s, (const uint64_t *)((uint8_t *)s + br),
-                        m_digits(bits), tab, g.stream);
+    cudaError_t e = ft::encrypt(ft::view_of(a), ft::view_of(b), n, (const uint8_t *)s,
+                                (const uint64_t *)((uint8_t *)s + br), m_digits(bits), tab, g.stream);
     if (e != cudaSuccess) {
         ft_array_free(a);
         ft_array_free(b);
