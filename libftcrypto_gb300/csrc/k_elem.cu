@@ -399,26 +399,32 @@ FT_DEV void fe_from_ref10(fe &f, const int32_t l[10])
     fe_sub(f, a, b);
 }
 
+// Each warp converts 32 consecutive points into shared memory (rows of 41
+// words: conflict-free) and writes their 5,120 contiguous bytes with
+// coalesced stores; one thread writing its 160-byte struct directly made
+// every store instruction of a warp touch 32 sectors.
 __global__ void __launch_bounds__(128) k_to_ref160(int32_t *out, const uint4 *p, size_t s, size_t n)
 {
-    FT_GRID_LOOP(i, n)
-    {
-        ge_p3 h;
-        ld_p3(h, p, s, i);
-        int32_t l[10];
-        int32_t *o = out + 40 * i;
-        fe_to_ref10(l, h.X);
-#pragma unroll
-        for (int j = 0; j < 10; ++j) o[j] = l[j];
-        fe_to_ref10(l, h.Y);
-#pragma unroll
-        for (int j = 0; j < 10; ++j) o[10 + j] = l[j];
-        fe_to_ref10(l, h.Z);
-#pragma unroll
-        for (int j = 0; j < 10; ++j) o[20 + j] = l[j];
-        fe_to_ref10(l, h.T);
-#pragma unroll
-        for (int j = 0; j < 10; ++j) o[30 + j] = l[j];
+    __shared__ int32_t stage[4][32 * 41];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int32_t *row = stage[warp] + 41 * lane;
+#pragma unroll 1
+    for (size_t base = (size_t)blockIdx.x * 128 + 32 * warp; base < n; base += (size_t)gridDim.x * 128) {
+        const size_t i = base + lane;
+        if (i < n) {
+            ge_p3 h;
+            ld_p3(h, p, s, i);
+            fe_to_ref10(row, h.X);
+            fe_to_ref10(row + 10, h.Y);
+            fe_to_ref10(row + 20, h.Z);
+            fe_to_ref10(row + 30, h.T);
+        }
+        __syncwarp();
+        const int words = 40 * (int)(n - base < 32 ? n - base : 32);
+        int32_t *o = out + 40 * base;
+#pragma unroll 1
+        for (int k = lane; k < words; k += 32) o[k] = stage[warp][41 * (k / 40) + k % 40];
+        __syncwarp();
     }
 }
 
