@@ -807,7 +807,7 @@ def run_ours(args):
 
 
 PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan", "segsum", "isum", "encode", "decode",
-                 "batch")
+                 "batch", "export")
 
 
 def run_profile(case: str) -> int:
@@ -885,6 +885,13 @@ def run_profile(case: str) -> int:
     elif case == "decode":
         enc = ft.Array.from_scalars(sc).to_bytes_folded()
         op = lambda: ft.Array.from_bytes_folded(enc)  # noqa: E731
+    elif case == "export":  # the e2e step's raw 160-byte export into pinned memory
+        a = ft.Array.init_point(n, base, 1)
+        a.mul_device(d_sc.data_ptr(), n)
+        out = torch.empty(n * 160, dtype=torch.uint8).pin_memory()
+        L = ft.api.lib()
+        import ctypes
+        op = lambda: ft.check(L.ft_array_to_bytes(ctypes.c_void_p(out.data_ptr()), out.numel(), a.handle))  # noqa: E731
     else:
         raise SystemExit(f"unknown case {case}")
     op()
