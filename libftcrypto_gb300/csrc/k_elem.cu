@@ -428,26 +428,39 @@ __global__ void __launch_bounds__(128) k_to_ref160(int32_t *out, const uint4 *p,
     }
 }
 
+// the mirror of k_to_ref160: each warp reads its 32 structs with coalesced
+// loads into shared memory, then each thread converts its own
 __global__ void __launch_bounds__(128) k_from_ref160(uint4 *p, size_t s, const int32_t *in, size_t n)
 {
-    FT_GRID_LOOP(i, n)
-    {
-        ge_p3 h;
-        int32_t l[10];
-        const int32_t *q = in + 40 * i;
+    __shared__ int32_t stage[4][32 * 41];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int32_t *row = stage[warp] + 41 * lane;
+#pragma unroll 1
+    for (size_t base = (size_t)blockIdx.x * 128 + 32 * warp; base < n; base += (size_t)gridDim.x * 128) {
+        const int words = 40 * (int)(n - base < 32 ? n - base : 32);
+        const int32_t *q = in + 40 * base;
+#pragma unroll 1
+        for (int k = lane; k < words; k += 32) stage[warp][41 * (k / 40) + k % 40] = q[k];
+        __syncwarp();
+        const size_t i = base + lane;
+        if (i < n) {
+            ge_p3 h;
+            int32_t l[10];
 #pragma unroll
-        for (int j = 0; j < 10; ++j) l[j] = q[j];
-        fe_from_ref10(h.X, l);
+            for (int j = 0; j < 10; ++j) l[j] = row[j];
+            fe_from_ref10(h.X, l);
 #pragma unroll
-        for (int j = 0; j < 10; ++j) l[j] = q[10 + j];
-        fe_from_ref10(h.Y, l);
+            for (int j = 0; j < 10; ++j) l[j] = row[10 + j];
+            fe_from_ref10(h.Y, l);
 #pragma unroll
-        for (int j = 0; j < 10; ++j) l[j] = q[20 + j];
-        fe_from_ref10(h.Z, l);
+            for (int j = 0; j < 10; ++j) l[j] = row[20 + j];
+            fe_from_ref10(h.Z, l);
 #pragma unroll
-        for (int j = 0; j < 10; ++j) l[j] = q[30 + j];
-        fe_from_ref10(h.T, l);
-        st_p3(p, s, i, h);
+            for (int j = 0; j < 10; ++j) l[j] = row[30 + j];
+            fe_from_ref10(h.T, l);
+            st_p3(p, s, i, h);
+        }
+        __syncwarp();
     }
 }
 

@@ -227,7 +227,8 @@ def test_export_into_pinned_memory(ft, orc):
 
 def test_large_exports_equal_concatenated_ranges(ft):
     """An export of 600,001 points equals the concatenated exports of three
-    sub-ranges (taken by get_range), in every format."""
+    sub-ranges (taken by get_range), in every format; the raw import of the
+    raw export gives the points back."""
     import ctypes
     g = synth.rng(14)
     n = 600_001
@@ -245,6 +246,9 @@ def test_large_exports_equal_concatenated_ranges(ft):
             ft.check(fn(w.ctypes.data_as(ctypes.c_void_p), w.size, p.handle))
             want.append(w)
         assert (got == np.concatenate(want)).all(), width
+        if width == 160:  # and the raw import of all of it gives the points back
+            back = ft.Array.from_bytes(got.reshape(n, 160))
+            assert (back.to_bytes_folded() == a.to_bytes_folded()).all()
 
 
 def test_constructors(ft, orc):
