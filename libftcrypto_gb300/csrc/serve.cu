@@ -314,7 +314,10 @@ void ftx_server_s::loop()
             admit(lk, q, sl);
         }
         if (stop && pending.empty() && running == 0) break;
-        cv_work.wait_for(lk, std::chrono::microseconds(200));
+        // submit, stop and every completion notify cv_work; with nothing
+        // queued or running the worker sleeps until one of them does
+        if (pending.empty() && running == 0) cv_work.wait(lk);
+        else cv_work.wait_for(lk, std::chrono::microseconds(200));
     }
 }
 
