@@ -148,8 +148,9 @@ ft_error ft_array_set_length(ft_ge25519_array array, size_t newlen);
 /* ftcrypto.h:314 */
 ft_error ft_array_mux(ft_ge25519_array iftrue, const int64_t *cond, const_ft_ge25519_array iffalse);
 
-/* ftcrypto.h:325 — compares canonical encodings (hash join on the host
- * instead of the reference's O(n*m) kernel) */
+/* ftcrypto.h:325 — compares canonical encodings (a device hash table of
+ * array2's encodings probed by array1's, instead of the reference's O(n*m)
+ * kernel) */
 ft_error ft_array_contains(int64_t *res, const_ft_ge25519_array array1, const_ft_ge25519_array array2);
 
 /* ftcrypto.h:334 — res[i] += summand[i]; res and summand may be the same

@@ -730,19 +730,37 @@ ft_error ft_array_mux(ft_ge25519_array iftrue, const int64_t *cond, const_ft_ge2
     return FT_ERR_NO_ERROR;
 }
 
+// res[i] = 1 iff array1[i] equals some point of array2 (ft_array_contains,
+// ftcrypto.cu:1046-1086, an O(n1 * n2) comparison there): the canonical
+// encodings of array2 go into a device hash table (the open-addressing
+// table decryption uses, keyed by encoding, valued by index) and those of
+// array1 are looked up in it, O(n1 + n2).  Equal encodings are equal points
+// on the curve.
 ft_error ft_array_contains(int64_t *res, const_ft_ge25519_array array1, const_ft_ge25519_array array2)
 {
     ENSURE_INIT();
-    size_t n1 = array1->n, n2 = array2->n;
-    std::vector<uint8_t> e1(n1 * 32), e2(n2 * 32);
-    ft_error err;
-    if ((err = ft_array_to_bytes_folded(e1.data(), e1.size(), array1))) return err;
-    if ((err = ft_array_to_bytes_folded(e2.data(), e2.size(), array2))) return err;
-    std::vector<const uint8_t *> keys(n2);
-    for (size_t j = 0; j < n2; ++j) keys[j] = e2.data() + 32 * j;
-    auto lt = [](const uint8_t *a, const uint8_t *b) { return std::memcmp(a, b, 32) < 0; };
-    std::sort(keys.begin(), keys.end(), lt);
-    for (size_t i = 0; i < n1; ++i) res[i] = std::binary_search(keys.begin(), keys.end(), e1.data() + 32 * i, lt);
+    const size_t n1 = array1->n, n2 = array2->n;
+    if (n1 == 0) return FT_ERR_NO_ERROR;
+    if (n2 == 0) {
+        std::memset(res, 0, n1 * sizeof(int64_t));
+        return FT_ERR_NO_ERROR;
+    }
+    if (n2 >= ((size_t)1 << 31)) return FT_ERR_BAD_SIZE;
+    uint64_t cap = 64;
+    while (cap < 2 * (uint64_t)n2) cap <<= 1;
+    const size_t b1 = align256(n1 * 32), b2 = align256(n2 * 32), bt = align256(ft::dlog_table_bytes(cap));
+    void *s;
+    CK(scratch(&s, b1 + b2 + bt + align256(n1 * 8)));
+    uint8_t *base = (uint8_t *)s;
+    uint8_t *e1 = base, *e2 = base + b1;
+    uint64_t *hit = (uint64_t *)(base + b1 + b2 + bt);
+    CK(ft::encode(e1, ft::view_of(array1), n1, g.stream));
+    CK(ft::encode(e2, ft::view_of(array2), n2, g.stream));
+    ft::DlogTable t;
+    CK(ft::dlog_build(t, base + b1 + b2, n2, cap, e2, g.stream));
+    CK(ft::dlog_lookup(hit, t, e1, n1, g.stream));
+    CK(d2h(res, hit, n1 * 8));
+    for (size_t i = 0; i < n1; ++i) res[i] = (uint64_t)res[i] != ~0ull ? 1 : 0;
     return FT_ERR_NO_ERROR;
 }
 

@@ -96,8 +96,9 @@ struct DlogTable {
     uint64_t m_max = 0, cap = 0;
 };
 size_t dlog_table_bytes(uint64_t cap);
-// fills a table laid out in `mem` (dlog_table_bytes(cap) bytes) from the
-// encodings of j*B, j < m_max, already at d_enc (m_max x 32 bytes)
+// fills a table laid out in `mem` (dlog_table_bytes(cap) bytes) mapping the
+// encodings at d_enc (m_max x 32 bytes) to their indices: j*B for
+// decryption, the points of an array for ft_array_contains
 cudaError_t dlog_build(DlogTable &t, void *mem, uint64_t m_max, uint64_t cap, const uint8_t *d_enc, cudaStream_t st);
 // m[i] = j where enc_i (n x 32 bytes) is the encoding of j*B, j < m_max; UINT64_MAX if none
 cudaError_t dlog_lookup(uint64_t *d_m, const DlogTable &t, const uint8_t *d_enc, size_t n, cudaStream_t st);

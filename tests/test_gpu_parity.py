@@ -92,6 +92,20 @@ def test_decode_golden(ft, golden):
         assert (one.validate() == -1) == bool(c["valid"]), i
 
 
+def test_contains_large_with_duplicates_and_empty(ft):
+    """ft_array_contains by the device hash table of encodings: membership of
+    k*B in {k'*B} is membership of k in {k'} (distinct k < L give distinct
+    points); duplicates, the identity (k = 0) and empty arrays included."""
+    g = synth.rng(16)
+    k2 = g.integers(0, 5000, 3000).astype(np.uint64)
+    k1 = g.integers(0, 8000, 5000).astype(np.uint64)
+    a1, a2 = ft.Array.from_small_scalars(k1), ft.Array.from_small_scalars(k2)
+    assert (a1.contains(a2) == np.isin(k1, k2).astype(np.int64)).all()
+    empty = ft.Array.init_scalar(0)
+    assert len(empty.contains(a2)) == 0
+    assert (a1.contains(empty) == 0).all()
+
+
 def test_off_curve_points_follow_the_formulas(ft, orc, golden):
     """Decoded points include the reference's results for rejected encodings
     (not on the curve); multiplication and addition still run the same field
