@@ -32,9 +32,16 @@ def build(force: bool = False) -> str:
 
 
 def build_ref() -> str | None:
-    """Build oracle/_ref/libftref.so from the reference sources, if present."""
+    """Build oracle/_ref/libftref.so from the reference sources, if present
+    (the recipe oracle/build_ref.sh knows where they lie)."""
     subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")])
     return REF_LIB_PATH if os.path.exists(REF_LIB_PATH) else None
+
+
+def ref_src() -> str:
+    """The reference's src/ directory as oracle/build_ref.sh resolves it
+    (FT_REF_SRC, else its default); it may not exist."""
+    return subprocess.check_output(["sh", os.path.join(HERE, "build_ref.sh"), "--src"], text=True).strip()
 
 
 def lib():
@@ -49,6 +56,7 @@ def lib():
         sig = {
             "fto_init": (I, []),
             "fto_encode": (None, [P, P, S]),
+            "fto_encode_mt": (None, [P, P, S, I]),
             "fto_decode": (ctypes.c_int64, [P, P, S]),
             "fto_to_affine": (None, [P, P, S]),
             "fto_from_affine": (None, [P, P, S]),
@@ -62,11 +70,14 @@ def lib():
             "fto_neg": (None, [P, S]),
             "fto_mul": (None, [P, P, S, I]),
             "fto_scale": (None, [P, P, S, I]),
+            "fto_scale_u64": (None, [P, ctypes.c_uint64, S, I]),
+            "fto_scale_u64_each": (None, [P, P, S, I]),
             "fto_index": (None, [P, P, S]),
             "fto_equal": (None, [P, P, P, S]),
             "fto_validate": (ctypes.c_int64, [P, S]),
             "fto_reduce": (None, [P, P, S, I]),
             "fto_scan": (None, [P, S, I]),
+            "fto_scan_mt": (None, [P, S, I, I]),
             "fto_segsum_csr": (None, [P, P, S, P, I]),
             "fto_isum": (I, [P, S, P, S, P]),
             "fto_encrypt": (I, [P, P, P, P, P, S, I]),
@@ -89,10 +100,16 @@ def _pts(n):
     return np.zeros((n, 128), dtype=np.uint8)
 
 
-def encode(pts: np.ndarray) -> np.ndarray:
+def encode(pts: np.ndarray, threads: int = 1) -> np.ndarray:
+    """Canonical encodings; threads > 1 uses the batched-inversion form
+    (fto_encode_mt), which gives the same bytes."""
+    pts = np.ascontiguousarray(pts)
     n = pts.shape[0]
     out = np.zeros((n, 32), dtype=np.uint8)
-    lib().fto_encode(_p(out), _p(pts), n)
+    if threads > 1:
+        lib().fto_encode_mt(_p(out), _p(pts), n, threads)
+    else:
+        lib().fto_encode(_p(out), _p(pts), n)
     return out
 
 
@@ -179,6 +196,23 @@ def scale(a, scalar, threads=1):
     return r
 
 
+def scale_u64(a, k: int, threads=1):
+    """k * a_i for a public k < 2^64 by double-and-add: the group element of
+    scale(a, k) (canonical encodings equal on the curve)."""
+    r = np.ascontiguousarray(a).copy()
+    lib().fto_scale_u64(_p(r), int(k), r.shape[0], threads)
+    return r
+
+
+def scale_u64_each(a, ks, threads=1):
+    """k_i * a_i for public k_i < 2^64, one per point, by double-and-add."""
+    r = np.ascontiguousarray(a).copy()
+    kk = np.ascontiguousarray(np.asarray(ks, dtype=np.uint64))
+    assert kk.shape[0] == r.shape[0]
+    lib().fto_scale_u64_each(_p(r), _p(kk), r.shape[0], threads)
+    return r
+
+
 def index(a):
     out = np.zeros(a.shape[0], dtype=np.int64)
     lib().fto_index(_p(out), _p(a), a.shape[0])
@@ -201,9 +235,14 @@ def reduce(a, threads=1):
     return out
 
 
-def scan(a, exclusive=False):
-    r = a.copy()
-    lib().fto_scan(_p(r), a.shape[0], 1 if exclusive else 0)
+def scan(a, exclusive=False, threads=1):
+    """Prefix sums; threads > 1 scans chunks in parallel (same group
+    elements, other projective coordinates: compare encodings)."""
+    r = np.ascontiguousarray(a).copy()
+    if threads > 1:
+        lib().fto_scan_mt(_p(r), r.shape[0], 1 if exclusive else 0, threads)
+    else:
+        lib().fto_scan(_p(r), r.shape[0], 1 if exclusive else 0)
     return r
 
 

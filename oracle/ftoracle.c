@@ -819,6 +819,59 @@ void fto_encode(uint8_t *out32, const uint8_t *pts, size_t n)
     }
 }
 
+/* The same canonical encodings as fto_encode, for large checks: each thread
+ * encodes a contiguous range, inverting the Z coordinates of 64 points at a
+ * time with one field inversion (Montgomery's simultaneous inversion:
+ * prefix products, one inversion, then the inverses peeled off backwards).
+ * A Z congruent to 0 is left out of the batch and gets the inverse 0, which
+ * is what fe_invert returns for it (0^(p-2) = 0), so every encoding equals
+ * ge_p3_tobytes's (sodium_ge.cu:382-394). */
+#define ENC_BATCH 64
+struct enc32_ctx { uint8_t *out; const uint8_t *pts; };
+
+static void encode_range(void *vctx, size_t lo, size_t hi)
+{
+    struct enc32_ctx *c = (struct enc32_ctx *)vctx;
+    ge_p3 p[ENC_BATCH];
+    fe pre[ENC_BATCH], inv[ENC_BATCH];
+    int zero[ENC_BATCH];
+    for (size_t b0 = lo; b0 < hi; b0 += ENC_BATCH) {
+        const size_t m = hi - b0 < ENC_BATCH ? hi - b0 : ENC_BATCH;
+        fe acc;
+        fe_1(&acc);
+        for (size_t j = 0; j < m; ++j) {
+            pt_load(&p[j], c->pts + 128 * (b0 + j));
+            zero[j] = fe_iszero(&p[j].Z);
+            pre[j] = acc; /* product of the non-zero Z before j */
+            if (!zero[j]) fe_mul(&acc, &acc, &p[j].Z);
+        }
+        fe r;
+        fe_invert(&r, &acc); /* 1 / (product of all non-zero Z) */
+        for (size_t j = m; j-- > 0;) {
+            if (zero[j]) {
+                fe_0(&inv[j]);
+                continue;
+            }
+            fe_mul(&inv[j], &r, &pre[j]); /* 1 / Z_j */
+            fe_mul(&r, &r, &p[j].Z);     /* 1 / (product of the non-zero Z before j) */
+        }
+        for (size_t j = 0; j < m; ++j) {
+            fe x, y;
+            uint8_t *s = c->out + 32 * (b0 + j);
+            fe_mul(&x, &p[j].X, &inv[j]);
+            fe_mul(&y, &p[j].Y, &inv[j]);
+            fe_tobytes(s, &y);
+            s[31] ^= (uint8_t)(fe_isnegative(&x) << 7);
+        }
+    }
+}
+
+void fto_encode_mt(uint8_t *out32, const uint8_t *pts, size_t n, int threads)
+{
+    struct enc32_ctx c = {out32, pts};
+    parallel_for(n, threads, encode_range, &c);
+}
+
 /* ftcrypto.cu:735-790: returns the last failing index, or -1 */
 int64_t fto_decode(uint8_t *pts, const uint8_t *in32, size_t n)
 {
@@ -1023,6 +1076,56 @@ void fto_scale(uint8_t *pts, const uint8_t *scalar, size_t n, int threads) /* ft
     parallel_for(n, threads, smul_range, &c);
 }
 
+/* k * P for a public k < 2^64 by left-to-right double-and-add (p3
+ * doubling, ge_addto for a set bit).  A faster stand-in for fto_scale with a
+ * small scalar when checking large arrays: on the curve it gives the same
+ * group element as the reference's ladder (ft_scale, ftcrypto.cu:966-983),
+ * in other projective coordinates; compare canonical encodings only. */
+struct scale64_ctx { uint8_t *pts; uint64_t k; };
+
+static void scale64_range(void *vctx, size_t lo, size_t hi)
+{
+    struct scale64_ctx *c = (struct scale64_ctx *)vctx;
+    int top = 63;
+    while (top >= 0 && !((c->k >> top) & 1)) --top;
+    for (size_t i = lo; i < hi; ++i) {
+        ge_p3 p, acc;
+        pt_load(&p, c->pts + 128 * i);
+        ge_zero(&acc);
+        for (int b = top; b >= 0; --b) {
+            ge_p1p1 t;
+            ge_p3_dbl(&t, &acc);
+            ge_p1p1_to_p3(&acc, &t);
+            if ((c->k >> b) & 1) ge_addto(&acc, &p);
+        }
+        pt_store(c->pts + 128 * i, &acc);
+    }
+}
+
+void fto_scale_u64(uint8_t *pts, uint64_t k, size_t n, int threads)
+{
+    struct scale64_ctx c = {pts, k};
+    parallel_for(n, threads, scale64_range, &c);
+}
+
+/* the same with a public k_i per point */
+struct scale64e_ctx { uint8_t *pts; const uint64_t *k; };
+
+static void scale64e_range(void *vctx, size_t lo, size_t hi)
+{
+    struct scale64e_ctx *c = (struct scale64e_ctx *)vctx;
+    for (size_t i = lo; i < hi; ++i) {
+        struct scale64_ctx one = {c->pts, c->k[i]};
+        scale64_range(&one, i, i + 1);
+    }
+}
+
+void fto_scale_u64_each(uint8_t *pts, const uint64_t *k, size_t n, int threads)
+{
+    struct scale64e_ctx c = {pts, k};
+    parallel_for(n, threads, scale64e_range, &c);
+}
+
 struct add_ctx { uint8_t *res; const uint8_t *other; int sub; };
 
 static void add_range(void *vctx, size_t lo, size_t hi)
@@ -1141,6 +1244,61 @@ void fto_scan(uint8_t *pts, size_t n, int exclusive)
             pt_store(pts + 128 * i, &acc);
         }
     }
+}
+
+/* fto_scan on `threads` threads, for large checks: each thread sums its
+ * contiguous chunk, the chunk totals are prefixed serially, then each thread
+ * rescans its chunk from its prefix.  The same group elements as the serial
+ * scan (other projective coordinates): compare canonical encodings. */
+struct scan_ctx { uint8_t *pts; size_t n; int threads; int exclusive; ge_p3 *part; int phase; };
+
+static void scan_range(void *vctx, size_t lo, size_t hi)
+{
+    struct scan_ctx *c = (struct scan_ctx *)vctx;
+    for (size_t t = lo; t < hi; ++t) {
+        size_t a = c->n * t / (size_t)c->threads, b = c->n * (t + 1) / (size_t)c->threads;
+        ge_p3 acc;
+        if (c->phase == 0) {
+            ge_zero(&acc);
+            for (size_t i = a; i < b; ++i) {
+                ge_p3 p;
+                pt_load(&p, c->pts + 128 * i);
+                ge_addto(&acc, &p);
+            }
+            c->part[t] = acc;
+            continue;
+        }
+        acc = c->part[t];
+        for (size_t i = a; i < b; ++i) {
+            ge_p3 p;
+            pt_load(&p, c->pts + 128 * i);
+            if (c->exclusive) {
+                pt_store(c->pts + 128 * i, &acc);
+                ge_addto(&acc, &p);
+            } else {
+                ge_addto(&acc, &p);
+                pt_store(c->pts + 128 * i, &acc);
+            }
+        }
+    }
+}
+
+void fto_scan_mt(uint8_t *pts, size_t n, int exclusive, int threads)
+{
+    if (threads < 1) threads = 1;
+    ge_p3 *part = (ge_p3 *)calloc((size_t)threads, sizeof(ge_p3));
+    struct scan_ctx c = {pts, n, threads, exclusive, part, 0};
+    parallel_for((size_t)threads, threads, scan_range, &c);
+    ge_p3 run;
+    ge_zero(&run);
+    for (int t = 0; t < threads; ++t) { /* exclusive prefix of the chunk totals */
+        ge_p3 tot = part[t];
+        part[t] = run;
+        ge_addto(&run, &tot);
+    }
+    c.phase = 1;
+    parallel_for((size_t)threads, threads, scan_range, &c);
+    free(part);
 }
 
 struct seg_ctx { uint8_t *out; const int32_t *off; const uint8_t *src; };

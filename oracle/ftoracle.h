@@ -31,6 +31,8 @@ int fto_init(void);
 /* canonical encode (ge25519_p3_tobytes) / decode (ge25519_frombytes) */
 void fto_encode(uint8_t *out32, const uint8_t *pts, size_t n);
 int64_t fto_decode(uint8_t *pts, const uint8_t *in32, size_t n);
+/* fto_encode on `threads` threads with batched inversion (same bytes) */
+void fto_encode_mt(uint8_t *out32, const uint8_t *pts, size_t n, int threads);
 
 /* affine (64 B: x || y) and reference-limb (160 B: 4 x 10 int32) formats */
 void fto_to_affine(uint8_t *out64, const uint8_t *pts, size_t n);
@@ -49,6 +51,11 @@ void fto_sub(uint8_t *res, const uint8_t *subtrahend, size_t n, int threads);
 void fto_neg(uint8_t *pts, size_t n);
 void fto_mul(uint8_t *pts, const uint8_t *scalars, size_t n, int threads);
 void fto_scale(uint8_t *pts, const uint8_t *scalar, size_t n, int threads);
+/* k * P_i for a public k < 2^64 by double-and-add (same group element as
+ * fto_scale; other projective coordinates) */
+void fto_scale_u64(uint8_t *pts, uint64_t k, size_t n, int threads);
+/* the same with a public k_i per point */
+void fto_scale_u64_each(uint8_t *pts, const uint64_t *k, size_t n, int threads);
 void fto_index(int64_t *res, const uint8_t *pts, size_t n);
 void fto_equal(int64_t *res, const uint8_t *a, const uint8_t *b, size_t n);
 int64_t fto_validate(const uint8_t *pts, size_t n);
@@ -56,6 +63,8 @@ int64_t fto_validate(const uint8_t *pts, size_t n);
 /* reductions */
 void fto_reduce(uint8_t *out, const uint8_t *pts, size_t n, int threads);
 void fto_scan(uint8_t *pts, size_t n, int exclusive);
+/* fto_scan on `threads` threads (chunk totals, then a rescan per chunk) */
+void fto_scan_mt(uint8_t *pts, size_t n, int exclusive, int threads);
 void fto_segsum_csr(uint8_t *out, const int32_t *offsets, size_t nseg,
                     const uint8_t *src, int threads);
 int fto_isum(uint8_t *res, size_t nres, const uint64_t *idxs, size_t n,

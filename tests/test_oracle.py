@@ -118,3 +118,47 @@ def test_against_libsodium(orc):
     a, b = enc[2], enc[3]
     s2 = orc.encode(orc.add(*(orc.decode(x[None])[0] for x in (a, b))))
     assert nb.crypto_core_ed25519_add(bytes(a), bytes(b)) == bytes(s2[0])
+
+
+def test_encode_mt_equals_encode(orc, golden):
+    """The batched-inversion encoder used for the full-size configuration
+    checks gives fto_encode's bytes: on-curve points, rejected decodes (off
+    the curve), zero Z and ragged batch edges (n not a multiple of 64)."""
+    g = synth.rng(13)
+    on = orc.from_scalars(synth.scalars_mod_L(g, 150), threads=4)
+    off, _ = orc.decode(hxs(c["in"] for c in golden["decode"]))
+    zz = on[:5].copy()
+    zz[:, 64:96] = 0                      # Z = 0
+    zz[1, 64:96] = 0xff                   # Z = 2^256 - 1 (not zero mod p)
+    zz[2, 64:96] = np.frombuffer(((1 << 255) - 19).to_bytes(32, "little"), dtype=np.uint8)  # Z = p
+    pts = np.concatenate([on, off, zz, on[::-1]])
+    want = orc.encode(pts)
+    for threads in (1, 2, 3, 16):
+        got = np.zeros_like(want)
+        orc.lib().fto_encode_mt(orc._p(got), orc._p(pts), pts.shape[0], threads)
+        assert (got == want).all()
+    assert (orc.encode(pts, threads=5) == want).all()
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 3, 1000, 65535, (1 << 32) - 1, (1 << 64) - 1])
+def test_scale_u64_equals_ladder(orc, k):
+    """Double-and-add by a public 64-bit k gives the reference ladder's group
+    element (the oracle's fto_scale, sodium_ge.cu:650-731)."""
+    g = synth.rng(14)
+    pts = orc.from_scalars(synth.scalars_mod_L(g, 21), threads=4)
+    want = orc.encode(orc.scale(pts, orc.small_to_scalars([k])[0]))
+    assert (orc.encode(orc.scale_u64(pts, k, threads=3)) == want).all()
+    ks = np.full(pts.shape[0], k, dtype=np.uint64)
+    ks[::2] = 7
+    each = orc.encode(orc.scale_u64_each(pts, ks, threads=4))
+    assert (each[1::2] == want[1::2]).all()
+    assert (each[::2] == orc.encode(orc.scale_u64(pts[::2], 7))).all()
+
+
+@pytest.mark.parametrize("exclusive", [False, True])
+def test_scan_mt_equals_serial_scan(orc, exclusive):
+    g = synth.rng(15)
+    pts = orc.from_scalars(synth.scalars_mod_L(g, 77), threads=4)
+    want = orc.encode(orc.scan(pts, exclusive))
+    for threads in (2, 5, 16, 100):
+        assert (orc.encode(orc.scan(pts, exclusive, threads=threads)) == want).all()

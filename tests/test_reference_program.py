@@ -10,10 +10,10 @@ import subprocess
 import pytest
 
 import libftcrypto_gb300 as lib
+import oracle
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), os.pardir))
-REF_SRC = os.environ.get("FT_REF_SRC", "/root/reference/src")
-PROGRAM = os.path.join(REF_SRC, "run_tests.cc")
+PROGRAM = os.path.join(oracle.ref_src(), "run_tests.cc")
 
 
 @pytest.mark.skipif(not os.path.isfile(PROGRAM), reason="reference sources absent")

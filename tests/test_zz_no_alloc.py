@@ -18,12 +18,17 @@ pytestmark = pytest.mark.gpu
 MAX_POINTS = 1048576  # FT_NOALLOC_SCAN_MAX_POINTS in include/ftcrypto_gb300.h
 
 
-def noalloc_scan(ft, arr, exclusive):
+def noalloc_scan(ft, arr, exclusive, stream=None):
+    """One call through the C ABI on `stream` (a stream the caller owns), or
+    on the library's stream; returns after the scan has finished."""
     L = ft.api.lib()
     planes, stride = arr.device_view()
+    ft.synchronize()  # the array's producer ran on the library's stream
     code = L.ftx_scan_noalloc(ctypes.c_void_p(planes), stride, len(arr), exclusive,
-                              ctypes.c_void_p(ft.stream_handle()))
+                              ctypes.c_void_p(stream.cuda_stream if stream is not None else ft.stream_handle()))
     ft.check(code)
+    if stream is not None:
+        stream.synchronize()
     ft.synchronize()
 
 
@@ -58,3 +63,31 @@ def test_noalloc_scan_largest_and_too_large(ft, orc):
     code = L.ftx_scan_noalloc(ctypes.c_void_p(planes), MAX_POINTS + 1, MAX_POINTS + 1, 0,
                               ctypes.c_void_p(ft.stream_handle()))
     assert code == 3  # FT_ERR_BAD_SIZE
+
+
+def test_noalloc_scan_on_callers_stream_allocates_nothing(ft, orc):
+    """The use the entry point exists for: the caller's own stream, and no
+    device memory taken by the call (the device's free memory, which any
+    cudaMalloc or growth of the library's pool would lower, is unchanged)."""
+    torch = pytest.importorskip("torch")
+    g = synth.rng(903)
+    n = 200_003
+    pts = orc.from_scalars(synth.scalars_mod_L(g, 4096), threads=8)
+    pts = np.tile(pts, (n // 4096 + 1, 1))[:n].copy()
+    ref = ft.Array.from_packed(pts)
+    ref.scan()
+    want = ref.to_bytes_folded()
+    st = torch.cuda.Stream()
+    for _ in range(2):  # the second call finds the first call's partial sums in the array
+        mine = ft.Array.from_packed(pts)
+        noalloc_scan(ft, mine, 0, st)  # first call on this device: the address lookup
+        free0, _ = ft.device_memory()
+        mine2 = ft.Array.from_packed(pts)
+        ft.synchronize()
+        free1, _ = ft.device_memory()
+        noalloc_scan(ft, mine2, 0, st)
+        free2, _ = ft.device_memory()
+        assert free2 == free1, "the call took device memory"
+        assert free1 <= free0
+        assert (mine.to_bytes_folded() == want).all()
+        assert (mine2.to_bytes_folded() == want).all()
