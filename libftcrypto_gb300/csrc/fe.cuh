@@ -113,6 +113,61 @@ FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
     for (int k = 0; k < 8; ++k) h.v[k] = r[k];
 }
 
+#ifndef FT_MUL_ALIGNED
+#define FT_MUL_ALIGNED 1
+#endif
+
+#if FT_MUL_ALIGNED
+// t = a * b (full 512-bit product).  Each product a_j * b_i is one 64-bit
+// window (lo at position p = i + j, hi at p + 1) that ptxas computes with
+// one IMAD.WIDE into an even-aligned register pair.  Windows at even p
+// accumulate in E (E[p], E[p + 1]); windows at odd p accumulate in O one
+// word lower (O[p - 1], O[p]), so that every window of both starts at an
+// even index.  Row i adds its four products of each parity as one carry
+// chain over consecutive windows, then its carry into the next word of that
+// accumulator; t = E + O * 2^32.  (The earlier form chained row i's even-j
+// products at positions i + j, odd for odd rows, and measured 60 MOV and 39
+// IMAD.MOV instructions per multiplication moving words between pairs.)
+FT_DEV void mul_wide(uint32_t t[16], const fe &a, const fe &b)
+{
+    uint32_t E[16], O[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) E[k] = O[k] = 0u;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const uint32_t bi = b.v[i];
+        // even p = i + j: j of the parity of i
+        const int je = i & 1;
+        E[i + je] = mad_lo_cc(a.v[je], bi, E[i + je]);
+        E[i + je + 1] = madc_hi_cc(a.v[je], bi, E[i + je + 1]);
+#pragma unroll
+        for (int j = je + 2; j < 8; j += 2) {
+            E[i + j] = madc_lo_cc(a.v[j], bi, E[i + j]);
+            E[i + j + 1] = madc_hi_cc(a.v[j], bi, E[i + j + 1]);
+        }
+        // the row's last window ends at E[i + je + 7]; the carry goes one
+        // word up (a word only carries have reached so far; E < 2^512, so
+        // past E[15] it is zero)
+        if (i + je + 8 < 16) E[i + je + 8] = addc(E[i + je + 8], 0u);
+        // odd p = i + j: j of the other parity, window at O[p - 1]
+        const int jo = je ^ 1;
+        O[i + jo - 1] = mad_lo_cc(a.v[jo], bi, O[i + jo - 1]);
+        O[i + jo] = madc_hi_cc(a.v[jo], bi, O[i + jo]);
+#pragma unroll
+        for (int j = jo + 2; j < 8; j += 2) {
+            O[i + j - 1] = madc_lo_cc(a.v[j], bi, O[i + j - 1]);
+            O[i + j] = madc_hi_cc(a.v[j], bi, O[i + j]);
+        }
+        if (i + jo + 7 < 16) O[i + jo + 7] = addc(O[i + jo + 7], 0u);
+    }
+    // t = E + O * 2^32 (O[15] is zero: its weight is 2^512)
+    t[0] = E[0];
+    t[1] = add_cc(E[1], O[0]);
+#pragma unroll
+    for (int k = 2; k < 15; ++k) t[k] = addc_cc(E[k], O[k - 1]);
+    t[15] = addc(E[15], O[14]);
+}
+#else
 // t = a * b (full 512-bit product).  Operand scanning with each row split
 // by the parity of the multiplicand limb: products a_j * b_i with j even are
 // chained into T as (lo, hi) pairs of the same product, j odd into U, and
@@ -159,7 +214,64 @@ FT_DEV void mul_wide(uint32_t t[16], const fe &a, const fe &b)
     for (int k = 2; k < 15; ++k) t[k] = addc_cc(T[k], U[k]);
     t[15] = addc(T[15], U[15]);
 }
+#endif
 
+#if FT_MUL_ALIGNED
+// t = a^2: the 28 cross products a_i a_j (i < j) as 64-bit windows in even
+// aligned register pairs, as in mul_wide: even p = i + j in T (T[p],
+// T[p + 1]), odd p in O one word lower (O[p - 1], O[p]); row i chains its
+// products of each parity.  t = 2 (T + O * 2^32) + the 8 squares a_i^2,
+// whose windows (2i, 2i + 1) form one chain.
+FT_DEV void sqr_wide(uint32_t t[16], const fe &a)
+{
+    uint32_t T[16], O[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) T[k] = O[k] = 0u;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        // j = i+1, i+3, ...: odd p, window at O[p - 1]
+        O[2 * i] = mad_lo_cc(a.v[i], a.v[i + 1], O[2 * i]);
+        O[2 * i + 1] = madc_hi_cc(a.v[i], a.v[i + 1], O[2 * i + 1]);
+#pragma unroll
+        for (int j = i + 3; j < 8; j += 2) {
+            O[i + j - 1] = madc_lo_cc(a.v[i], a.v[j], O[i + j - 1]);
+            O[i + j] = madc_hi_cc(a.v[i], a.v[j], O[i + j]);
+        }
+        {
+            const int last = i + 1 + 2 * ((6 - i) / 2);
+            if (i + last + 2 < 16) O[i + last + 1] = addc(O[i + last + 1], 0u);
+        }
+        // j = i+2, i+4, ...: even p
+        if (i < 6) {
+            T[2 * i + 2] = mad_lo_cc(a.v[i], a.v[i + 2], T[2 * i + 2]);
+            T[2 * i + 3] = madc_hi_cc(a.v[i], a.v[i + 2], T[2 * i + 3]);
+#pragma unroll
+            for (int j = i + 4; j < 8; j += 2) {
+                T[i + j] = madc_lo_cc(a.v[i], a.v[j], T[i + j]);
+                T[i + j + 1] = madc_hi_cc(a.v[i], a.v[j], T[i + j + 1]);
+            }
+            const int last = i + 2 + 2 * ((5 - i) / 2);
+            if (i + last + 2 < 16) T[i + last + 2] = addc(T[i + last + 2], 0u);
+        }
+    }
+    // the cross products sum to less than a^2 / 2 < 2^511: no carry out
+    uint32_t c[16];
+    c[0] = T[0];
+    c[1] = add_cc(T[1], O[0]);
+#pragma unroll
+    for (int k = 2; k < 16; ++k) c[k] = addc_cc(T[k], O[k - 1]);
+    t[0] = add_cc(c[0], c[0]);
+#pragma unroll
+    for (int k = 1; k < 16; ++k) t[k] = addc_cc(c[k], c[k]);
+    t[0] = mad_lo_cc(a.v[0], a.v[0], t[0]);
+    t[1] = madc_hi_cc(a.v[0], a.v[0], t[1]);
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+        t[2 * i] = madc_lo_cc(a.v[i], a.v[i], t[2 * i]);
+        t[2 * i + 1] = madc_hi_cc(a.v[i], a.v[i], t[2 * i + 1]);
+    }
+}
+#else
 // t = a^2: the 28 cross products a_i a_j (i < j) are chained as (lo, hi)
 // pairs of the same product, split by the parity of i + j as in mul_wide
 // (even into T, odd into U); t = 2 (T + U) + the 8 squares, which form one
@@ -213,6 +325,8 @@ FT_DEV void sqr_wide(uint32_t t[16], const fe &a)
         t[2 * i + 1] = madc_hi_cc(a.v[i], a.v[i], t[2 * i + 1]);
     }
 }
+
+#endif
 
 FT_DEV void fe_mul(fe &h, const fe &a, const fe &b)
 {

@@ -58,6 +58,13 @@ void hc_fe_mul(uint32_t *h, const uint32_t *a, const uint32_t *b)
     fe_mul(z, x, y);
     memcpy(h, z.v, 32);
 }
+void hc_mul_wide(uint32_t *t, const uint32_t *a, const uint32_t *b)
+{
+    fe x, y;
+    memcpy(x.v, a, 32); memcpy(y.v, b, 32);
+    mul_wide(t, x, y);
+}
+void hc_sqr_wide(uint32_t *t, const uint32_t *a) { fe x; memcpy(x.v, a, 32); sqr_wide(t, x); }
 void hc_fe_sq(uint32_t *h, const uint32_t *a) { fe x, z; memcpy(x.v, a, 32); fe_sq(z, x); memcpy(h, z.v, 32); }
 void hc_fe_add(uint32_t *h, const uint32_t *a, const uint32_t *b) { fe x, y, z; memcpy(x.v, a, 32); memcpy(y.v, b, 32); fe_add(z, x, y); memcpy(h, z.v, 32); }
 void hc_fe_sub(uint32_t *h, const uint32_t *a, const uint32_t *b) { fe x, y, z; memcpy(x.v, a, 32); memcpy(y.v, b, 32); fe_sub(z, x, y); memcpy(h, z.v, 32); }

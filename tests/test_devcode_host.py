@@ -57,6 +57,27 @@ def test_field_ops(hc):
         assert v(out) % P == pow(a, P - 2, P)
 
 
+def test_wide_products_exact(hc):
+    """mul_wide / sqr_wide return the exact 512-bit product (so the fold, and
+    every coordinate after it, is the same whatever the accumulation order):
+    random operands, limbs of all ones, single set limbs."""
+    rnd = random.Random(9)
+    M = 2**256 - 1
+    vals = [0, 1, M, M - 1, 2**255, 2**224, 2**32 - 1, (2**32 - 1) << 224]
+    vals += [sum(((2**32 - 1) if (m >> k) & 1 else 0) << (32 * k) for k in range(8)) for m in range(0, 256, 7)]
+    vals += [rnd.getrandbits(256) for _ in range(3000)]
+    t = (ctypes.c_uint32 * 16)()
+
+    def v16(x):
+        return sum(int(x[i]) << (32 * i) for i in range(16))
+    for i, a in enumerate(vals):
+        b = vals[(11 * i + 5) % len(vals)]
+        hc.hc_mul_wide(t, w(a), w(b))
+        assert v16(t) == a * b
+        hc.hc_sqr_wide(t, w(a))
+        assert v16(t) == a * a
+
+
 def test_group_and_smul(hc, orc):
     g = synth.rng(3)
     n = 48
