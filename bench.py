@@ -178,7 +178,8 @@ def profile_traffic():
 # ---------------------------------------------------------------- our arm
 
 def imad_peak(sm_count: int):
-    """32x32->64 multiply-accumulates per second (libftbench.so probe)."""
+    """32x32->64 products per second of the mad.wide.u32 probe alone
+    (libftbench.so; its ncu summary is profiles/k_imad_wide_peak.md)."""
     import ctypes
     lib = ctypes.CDLL(os.path.join(ROOT, "libftcrypto_gb300", "libftbench.so"))
     lib.ftb_imad_wide_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
@@ -186,6 +187,34 @@ def imad_peak(sm_count: int):
     if lib.ftb_imad_wide_peak(ctypes.byref(v), sm_count) != 0:
         return None
     return v.value
+
+
+def int_peaks(sm_count: int, gpu_index: int, seconds: float = 1.5):
+    """The integer-pipe probes of libftbench.so (csrc/bench_peak.cu), repeated
+    for `seconds` while nvidia-smi samples the SM clock; best of all runs, in
+    32x32->64 products per second: mad.wide.u32 (one instruction per
+    product), mad.lo.u32 (two per product) and the library's own field
+    multiplication (64 products each).  `peak` is the higher of the two
+    instruction probes; per_sm_clk divides it by SMs x the sampled clock."""
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(ROOT, "libftcrypto_gb300", "libftbench.so"))
+    lib.ftb_int_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int]
+    v = (ctypes.c_double * 3)()
+    best = [0.0, 0.0, 0.0]
+    with Clocks(gpu_index) as ck:
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            if lib.ftb_int_peaks(v, sm_count, 3) != 0:
+                return None
+            best = [max(b, x) for b, x in zip(best, v)]
+    clk = ck.summary()
+    peak = max(best[0], best[1])
+    out = {"peak": peak, "imad_wide": best[0], "imad_lo_pairs": best[1], "fe_mul": best[2],
+           "sm_mhz": clk["sm_mhz"], "clock_samples": clk["samples"], "clock_reasons": clk["reasons"]}
+    if clk["sm_mhz"]:
+        out["per_sm_clk"] = peak / (sm_count * clk["sm_mhz"] * 1e6)
+        out["fe_mul_per_sm_clk"] = best[2] / (sm_count * clk["sm_mhz"] * 1e6)
+    return out
 
 
 def to_i64(a: np.ndarray) -> np.ndarray:
@@ -350,10 +379,17 @@ def timed(ev, fn, reps, flush=None):
 
 
 def roof(bytes_alg, products, ms, hbm_peak, imad):
+    """HBM and integer fractions of one timed operation.  hbm_ceiling is the
+    HBM fraction the operation reaches when the integer pipe runs at `imad`
+    (its bytes per product x the integer peak, over the HBM peak, at most
+    1); frac_of_ceiling = hbm_frac / hbm_ceiling (= int_frac below 1)."""
     gbs = bytes_alg / (ms * 1e-3) / 1e9
     r = {"bound": "int", "hbm_achieved_gbs": round(gbs, 1), "hbm_frac": round(gbs / hbm_peak, 4)}
     if imad:
         r["int_frac"] = round(products / (ms * 1e-3) / imad, 4)
+        ceiling = min(1.0, bytes_alg / products * imad / 1e9 / hbm_peak)
+        r["hbm_ceiling"] = round(ceiling, 4)
+        r["frac_of_ceiling"] = round(gbs / hbm_peak / ceiling, 4)
     return r
 
 
@@ -367,7 +403,21 @@ def decrypt_matches(ft, c1, c2, sk, msum):
     return bool(b.equal(want).all())
 
 
+def oracle_check(pairs):
+    """(got, want) pairs of canonical encodings -> {bit_exact_vs_oracle,
+    outputs_compared, mismatches}."""
+    bad = sum(int((g != w).any(axis=1).sum()) for g, w in pairs)
+    n = sum(int(w.shape[0]) for _, w in pairs)
+    return {"bit_exact_vs_oracle": bad == 0, "outputs_compared": n, "mismatches": bad}
+
+
 def extras(ft, synth, torch, st, hbm_peak, imad):
+    """The secondary configurations: each timed (CUDA events on the library's
+    stream, median of 11), and each output of its first run compared with
+    the oracle's canonical encodings (the oracle on all host cores; inputs
+    encrypted on the GPU are exported to it in the packed layout)."""
+    import oracle
+    thr = os.cpu_count() or 1
     ev = Ev(st)
     flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -388,34 +438,35 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
         torch.cuda.synchronize()
         c1, c2 = ft.Array.init_scalar(n), ft.Array.init_scalar(n)
         ft.encrypt_device(c1, c2, pk, d_m.data_ptr(), d_r.data_ptr(), n, nbits)
-        return c1, c2
+        return c1, c2, r
 
     # ciphertext add: two arrays of 65,536 ciphertexts, m in {0,1}
     n1 = 1 << 16
     ma, mb = synth.plaintexts(g, n1, 1), synth.plaintexts(g, n1, 1)
-    a1, a2 = encrypt_dev(ma)
-    b1, b2 = encrypt_dev(mb)
+    a1, a2, ra = encrypt_dev(ma)
+    b1, b2, rb = encrypt_dev(mb)
     s1, s2 = a1.get_range(0, n1, 1), a2.get_range(0, n1, 1)
     ft.ct_add(s1, s2, b1, b2)
     ok = decrypt_matches(ft, s1, s2, sk[0], ma + mb)
+    oa1, oa2 = oracle.encrypt(pk, ma, ra, threads=thr)
+    ob1, ob2 = oracle.encrypt(pk, mb, rb, threads=thr)
+    chk = oracle_check([(s1.to_bytes_folded(), oracle.encode(oracle.add(oa1, ob1, thr), thr)),
+                        (s2.to_bytes_folded(), oracle.encode(oracle.add(oa2, ob2, thr), thr))])
+    del oa1, oa2, ob1, ob2, s1, s2
     ms = timed(ev, lambda: ft.ct_add(a1, a2, b1, b2), 11, flush)
     out["ct_add_65536"] = {"ct_adds_per_s": n1 / (ms * 1e-3), "ms": ms, "decrypt_check": ok, "l2": "flushed",
-                           **roof(2 * n1 * 3 * B_PT, 2 * n1 * W_ALG_PTADD, ms, hbm_peak, imad)}
+                           **chk, **roof(2 * n1 * 3 * B_PT, 2 * n1 * W_ALG_PTADD, ms, hbm_peak, imad)}
+    del a1, a2, b1, b2
 
-    # full sum of 16,777,216 ciphertexts
+    # full sum and segmented sum of 16,777,216 ciphertexts
     n3 = 1 << 24
+    nseg = 1 << 20
     m3 = synth.plaintexts(g, n3, 1)
-    c1, c2 = encrypt_dev(m3)
+    c1, c2, _ = encrypt_dev(m3)
     r1, r2 = ft.Array.init_scalar(1), ft.Array.init_scalar(1)
     c1.reduce_into(r1, 0)
     c2.reduce_into(r2, 0)
     ok = decrypt_matches(ft, r1, r2, sk[0], [int(m3.sum())])
-    ms = timed(ev, lambda: (c1.reduce_into(r1, 0), c2.reduce_into(r2, 0)), 11)
-    out["reduce_16M_ct"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok,
-                            **roof(2 * n3 * B_PT, 2 * n3 * W_ALG_PTADD, ms, hbm_peak, imad)}
-
-    # segmented sum of the same 16,777,216 into 1,048,576 CSR segments
-    nseg = 1 << 20
     off = synth.csr_offsets(g, n3, nseg)
     d_off = torch.from_numpy(off).cuda()
     torch.cuda.synchronize()
@@ -423,30 +474,82 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     ft.segmented_sum_csr_device(o1, d_off.data_ptr(), nseg, c1)
     ft.segmented_sum_csr_device(o2, d_off.data_ptr(), nseg, c2)
     segm = np.add.reduceat(m3, off[:-1]).astype(np.uint64)
-    ok = decrypt_matches(ft, o1, o2, sk[0], segm)
+    ok_seg = decrypt_matches(ft, o1, o2, sk[0], segm)
+    red_pairs, seg_pairs = [], []
+    for c, r, o in ((c1, r1, o1), (c2, r2, o2)):
+        pts = c.to_packed()
+        red_pairs.append((r.to_bytes_folded(), oracle.encode(oracle.reduce(pts, thr))))
+        seg_pairs.append((o.to_bytes_folded(), oracle.encode(oracle.segsum_csr(off, pts, thr), thr)))
+        del pts
+    ms = timed(ev, lambda: (c1.reduce_into(r1, 0), c2.reduce_into(r2, 0)), 11)
+    out["reduce_16M_ct"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok, **oracle_check(red_pairs),
+                            **roof(2 * n3 * B_PT, 2 * n3 * W_ALG_PTADD, ms, hbm_peak, imad)}
     ms = timed(ev, lambda: (ft.segmented_sum_csr_device(o1, d_off.data_ptr(), nseg, c1),
                             ft.segmented_sum_csr_device(o2, d_off.data_ptr(), nseg, c2)), 11)
     seg_bytes = 2 * (n3 * B_PT + nseg * B_PT) + (nseg + 1) * 4
-    out["segsum_16M_ct_1M_seg"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok,
+    out["segsum_16M_ct_1M_seg"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok_seg,
+                                   **oracle_check(seg_pairs),
                                    **roof(seg_bytes, 2 * (n3 - nseg) * W_ALG_PTADD, ms, hbm_peak, imad)}
-    del c1, c2, o1, o2
+    del c1, c2, o1, o2, red_pairs, seg_pairs
 
     # inclusive scan of 4,194,304 ciphertexts
     n4 = 1 << 22
     m4 = synth.plaintexts(g, n4, 1)
-    c1, c2 = encrypt_dev(m4)
+    c1, c2, _ = encrypt_dev(m4)
     t1, t2 = c1.get_range(0, n4, 1), c2.get_range(0, n4, 1)
-    t1.scan()
-    t2.scan()
+    ft.ct_scan(t1, t2)
     idx = np.sort(g.choice(n4, 64, replace=False))
     ok = decrypt_matches(ft, t1.get_subset(idx), t2.get_subset(idx), sk[0], np.cumsum(m4)[idx])
-    ms = timed(ev, lambda: (t1.scan(), t2.scan()), 11)
-    out["scan_4M_ct"] = {"ct_per_s": n4 / (ms * 1e-3), "ms": ms, "decrypt_check_sample": ok,
+    pairs = [(t.to_bytes_folded(), oracle.encode(oracle.scan(c.to_packed(), False, thr), thr))
+             for t, c in ((t1, c1), (t2, c2))]
+    ms = timed(ev, lambda: ft.ct_scan(t1, t2), 11)
+    out["scan_4M_ct"] = {"ct_per_s": n4 / (ms * 1e-3), "ms": ms, "decrypt_check_sample": ok, **oracle_check(pairs),
+                         "call": "ftx_ct_scan (both halves of the ciphertexts in one call)",
                          **roof(2 * n4 * 2 * B_PT, 2 * n4 * W_ALG_PTADD, ms, hbm_peak, imad)}
-    del c1, c2, t1, t2
+    ms1 = timed(ev, lambda: t1.scan(), 11)
+    out["scan_4M_ct"]["one_half_ft_array_scan_ms"] = ms1
+    del c1, c2, t1, t2, pairs
     out["batched_uneven_4096"] = uneven_batch(ft, synth, torch, st)
     out["serving"] = serving(ft, synth, torch)
     return out
+
+
+def uneven_expected(oracle, pool, work, offs, thr):
+    """The oracle's canonical encodings of every output of the uneven mix, in
+    the order of uneven_outputs: per array c1's outputs then c2's.  Arrays of
+    one kind are concatenated into one oracle call (segment offsets shifted;
+    scaling by a public k_i per point)."""
+    P = pool.shape[0]
+    parts = {}
+    for kind in ("add", "scale", "segsum"):
+        idx = [i for i, w in enumerate(work) if w["op"] == kind]
+        if not idx:
+            continue
+        xs = [pool[offs[i]:offs[i] + work[i]["len"]] for i in idx] + \
+             [pool[P - work[i]["len"] - offs[i]:P - offs[i]] for i in idx]
+        x = np.concatenate(xs)
+        if kind == "add":
+            ys = [pool[0:work[i]["len"]] for i in idx] + [pool[P - work[i]["len"]:P] for i in idx]
+            res = oracle.add(x, np.concatenate(ys), thr)
+            lens = [work[i]["len"] for i in idx] * 2
+        elif kind == "scale":
+            ks = np.concatenate([np.full(work[i]["len"], work[i]["k"], np.uint64) for i in idx] * 2)
+            res = oracle.scale_u64_each(x, ks, thr)
+            lens = [work[i]["len"] for i in idx] * 2
+        else:
+            offl, base = [np.zeros(1, np.int64)], 0
+            for j in list(idx) * 2:
+                o = work[j]["offsets"].astype(np.int64)
+                offl.append(o[1:] + base)
+                base += int(o[-1])
+            res = oracle.segsum_csr(np.concatenate(offl).astype(np.int32), x, thr)
+            lens = [len(work[i]["offsets"]) - 1 for i in idx] * 2
+        enc = oracle.encode(res, thr)
+        cuts = np.cumsum([0] + lens)
+        per = [enc[cuts[j]:cuts[j + 1]] for j in range(len(lens))]
+        for q, i in enumerate(idx):
+            parts[i] = (per[q], per[q + len(idx)])
+    return [parts[i] for i in range(len(work))]
 
 
 def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=5):
@@ -454,16 +557,22 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=5):
     one op (add 40%, scale by k in [1,1000] 30%, segmented sum of mean-8
     segments 30%): one persistent launch replayed from a CUDA graph against
     one library call per array (ft_add / ftx_scale_bounded /
-    ftx_segmented_sum_csr_device, two per ciphertext array)."""
+    ftx_segmented_sum_csr_device, two per ciphertext array).  Before timing,
+    both forms run once on copies of all 4,096 arrays and every output of
+    both is compared with the oracle."""
+    import oracle
+    thr = os.cpu_count() or 1
     ev = Ev(st)
     g = synth.rng(SEED + 11)
     work = synth.uneven_mix(g, n_arrays=n_arrays)
     pool = 1 << 17
-    base = ft.Array.from_scalars(synth.scalars_mod_L(g, pool))
-    arrs, dev_off = [], []
+    pool_sc = synth.scalars_mod_L(g, pool)
+    base = ft.Array.from_scalars(pool_sc)
+    arrs, offs = [], []
     for w in work:
         n = w["len"]
         o = int(g.integers(0, pool - n + 1))
+        offs.append(o)
         c1, c2 = base.get_range(o, o + n, 1), base.get_range(pool - n - o, pool - o, 1)
         ex = {}
         if w["op"] == "add":
@@ -502,24 +611,33 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=5):
                 b.segmented_sum(ex["o2"], w["offsets"], c2)
         return b
 
-    # bit-exact: both forms on copies of the first 256 arrays
     def cp(a):
         return a.get_range(0, len(a), 1)
-    sub = list(zip(work, arrs))[:256]
-    s_plain = [(w, (cp(c1), cp(c2), {k: (cp(v) if k != "doff" else v) for k, v in ex.items()})) for w, (c1, c2, ex) in sub]
-    s_batch = [(w, (cp(c1), cp(c2), {k: (cp(v) if k != "doff" else v) for k, v in ex.items()})) for w, (c1, c2, ex) in sub]
-    plain(s_plain)
-    sb = batch_of(s_batch)
-    sb.run()
 
     def outs(pairs):
         r = []
         for w, (c1, c2, ex) in pairs:
-            r += [ex["o1"], ex["o2"]] if w["op"] == "segsum" else [c1, c2]
+            r.append([ex["o1"], ex["o2"]] if w["op"] == "segsum" else [c1, c2])
         return r
-    same = all((x.to_bytes_folded() == y.to_bytes_folded()).all() for x, y in zip(outs(s_plain), outs(s_batch)))
-    sb.free()
-    del s_plain, s_batch
+
+    # bit-exact: both forms on copies of every array, every output against the oracle
+    want = uneven_expected(oracle, oracle.from_scalars(pool_sc, threads=thr), work, offs, thr)
+    forms = {}
+    for name in ("batched", "plain"):
+        sub = [(w, (cp(c1), cp(c2), {k: (cp(v) if k != "doff" else v) for k, v in ex.items()}))
+               for w, (c1, c2, ex) in zip(work, arrs)]
+        if name == "plain":
+            plain(sub)
+        else:
+            sb = batch_of(sub)
+            sb.run()
+        pairs = []
+        for (x1, x2), (w1, w2) in zip(outs(sub), want):
+            pairs += [(x1.to_bytes_folded(), w1), (x2.to_bytes_folded(), w2)]
+        forms[name] = oracle_check(pairs)
+        if name == "batched":
+            sb.free()
+        del sub, pairs
 
     b = batch_of(list(zip(work, arrs)))
     b.run()  # uploads the work list and captures the graph
@@ -532,22 +650,48 @@ def uneven_batch(ft, synth, torch, st, n_arrays=4096, reps=5):
     n_ct = int(sum(w["len"] for w in work))
     return {"arrays": n_arrays, "ciphertexts": n_ct, "ops": n_ops, "work_items": n_items,
             "batched_graph_ms": ms_batch, "plain_per_array_ms": ms_plain, "speedup": ms_plain / ms_batch,
-            "batched_ct_per_s": n_ct / (ms_batch * 1e-3), "bit_exact_batched_vs_plain_256_arrays": bool(same),
-            "launches": {"batched": 1, "plain": 2 * n_arrays}}
+            "batched_ct_per_s": n_ct / (ms_batch * 1e-3),
+            "bit_exact_vs_oracle": forms["batched"]["bit_exact_vs_oracle"] and forms["plain"]["bit_exact_vs_oracle"],
+            "outputs_compared": forms["batched"]["outputs_compared"] + forms["plain"]["outputs_compared"],
+            "oracle_check": forms, "launches": {"batched": 1, "plain": 2 * n_arrays}}
 
 
 SMALL_REQ = 65536  # "small" requests in the serving report: at most this many ciphertexts
 
 
-def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slots=8):
+SERVING_LOADS = (0.1, 0.3, 0.5, 0.7, 0.9, 1.0)
+SERVING_LIVE_PLAIN = (0.5, 0.9)
+
+
+def fifo_latencies(arrivals, service):
+    """Latencies (arrival -> done) of one-at-a-time FIFO service: the plain
+    drop-in called once per request by one caller (Lindley's recursion)."""
+    lat, free_at = [], 0.0
+    for a, s in zip(arrivals, service):
+        start = max(a, free_at)
+        free_at = start + s
+        lat.append(free_at - a)
+    return np.array(lat)
+
+
+def serving(ft, synth, torch, loads=SERVING_LOADS, n_req=400, budget=120 << 30, slots=8,
+            live_plain=SERVING_LIVE_PLAIN):
     """Serving: requests of 1,024..4,194,304 ciphertexts (log-uniform), mix
     35% encrypt of {0,1}, 25% re-randomise, 20% variable-base scalar-mult
     mod L, 20% segmented sum of mean-32 segments; Poisson arrivals at a
-    fraction of the measured capacity; 120 GB admission budget.  p50 / p99
-    latency (arrival -> GPU work complete), also over the small requests
-    (<= SMALL_REQ ciphertexts), and throughput, for the server (continuous
-    batching over `slots` streams, half of them express) and for the plain
-    drop-in called once per request on the same arrival schedule."""
+    fraction of the measured capacity; 120 GB admission budget.  One set of
+    n_req requests, replayed at every offered load on its own Poisson
+    schedule.  p50 / p99 latency (arrival -> GPU work complete), also over
+    the small requests (<= SMALL_REQ ciphertexts), and throughput:
+      server            live, continuous batching over `slots` streams (half
+                        express), outputs released as soon as collected;
+      plain_per_request the drop-in called once per request in arrival
+                        order: each request's service time measured alone
+                        (GPU work complete, host copies included), the
+                        latencies of the arrival schedule by the FIFO
+                        recursion (one caller, one request at a time);
+      plain_live        the same loop run live at the loads in live_plain,
+                        to show that the recursion matches it."""
     import threading
     g = synth.rng(SEED + 21)
     sk = synth.scalars_mod_L(g, 1)
@@ -559,20 +703,20 @@ def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slot
     c_pool = ft.encrypt(pk, m_pool, r_pool, 1)
     ops = ("encrypt", "rerand", "smul", "segsum")
 
-    def make_reqs(n):
-        out = []
-        for _ in range(n):
-            op = ops[int(g.choice(4, p=[0.35, 0.25, 0.2, 0.2]))]
-            size = int(np.floor(np.exp(g.uniform(np.log(1024), np.log(NMAX)))))
-            o = int(g.integers(0, NMAX - size + 1))
-            req = {"op": op, "n": size, "o": o}
-            if op in ("rerand", "smul", "segsum"):
-                req["c"] = (c_pool[0].get_range(o, o + size, 1), c_pool[1].get_range(o, o + size, 1))
-            if op == "segsum":
-                req["off"] = synth.csr_offsets(g, size, max(1, size // 32))
-            out.append(req)
-        ft.synchronize()
-        return out
+    reqs = []
+    for _ in range(n_req):
+        op = ops[int(g.choice(4, p=[0.35, 0.25, 0.2, 0.2]))]
+        size = int(np.floor(np.exp(g.uniform(np.log(1024), np.log(NMAX)))))
+        o = int(g.integers(0, NMAX - size + 1))
+        req = {"op": op, "n": size, "o": o}
+        if op in ("rerand", "smul", "segsum"):
+            req["c"] = (c_pool[0].get_range(o, o + size, 1), c_pool[1].get_range(o, o + size, 1))
+        if op == "segsum":
+            req["off"] = synth.csr_offsets(g, size, max(1, size // 32))
+        reqs.append(req)
+    ft.synchronize()
+    small = np.array([q["n"] <= SMALL_REQ for q in reqs])
+    ct = sum(q["n"] for q in reqs)
 
     def submit(srv, q):
         n, o = q["n"], q["o"]
@@ -584,7 +728,7 @@ def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slot
             return srv.submit_smul(*q["c"], k_pool[o:o + n])
         return srv.submit_segsum(*q["c"], q["off"])
 
-    def run_server(reqs, arrivals):
+    def run_server(arrivals):
         srv = ft.Server(pk, budget, slots)
         tickets, lat = [], []
         done = threading.Event()
@@ -595,6 +739,8 @@ def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slot
                     time.sleep(0.0001)
                 c1, c2, _, ms = srv.wait(tickets[i])
                 lat.append(ms)
+                if reqs[i]["op"] in ("encrypt", "segsum"):
+                    srv.release(c1, c2)
             done.set()
         th = threading.Thread(target=waiter)
         th.start()
@@ -610,50 +756,62 @@ def serving(ft, synth, torch, loads=(0.5, 0.9), n_req=80, budget=120 << 30, slot
         srv.close()
         return np.array(lat), wall
 
-    def run_plain(reqs, arrivals):
+    def plain_call(q):
+        n, o = q["n"], q["o"]
+        if q["op"] == "encrypt":
+            out = ft.encrypt(pk, m_pool[o:o + n], r_pool[o:o + n], 1)
+        elif q["op"] == "rerand":
+            ft.rerandomise(q["c"][0], q["c"][1], pk, r_pool[o:o + n])
+        elif q["op"] == "smul":
+            q["c"][0].mul(k_pool[o:o + n])
+            q["c"][1].mul(k_pool[o:o + n])
+        else:
+            out = (ft.segmented_sum_csr(q["off"], q["c"][0]), ft.segmented_sum_csr(q["off"], q["c"][1]))
+        ft.synchronize()
+
+    def run_plain(arrivals):
         lat = []
         t0 = time.perf_counter()
         for q, a in zip(reqs, arrivals):
             d = t0 + a - time.perf_counter()
             if d > 0:
                 time.sleep(d)
-            n, o = q["n"], q["o"]
-            if q["op"] == "encrypt":
-                out = ft.encrypt(pk, m_pool[o:o + n], r_pool[o:o + n], 1)
-            elif q["op"] == "rerand":
-                ft.rerandomise(q["c"][0], q["c"][1], pk, r_pool[o:o + n])
-            elif q["op"] == "smul":
-                q["c"][0].mul(k_pool[o:o + n])
-                q["c"][1].mul(k_pool[o:o + n])
-            else:
-                out = (ft.segmented_sum_csr(q["off"], q["c"][0]), ft.segmented_sum_csr(q["off"], q["c"][1]))
-            ft.synchronize()
+            plain_call(q)
             lat.append((time.perf_counter() - (t0 + a)) * 1e3)
         return np.array(lat), time.perf_counter() - t0
 
+    def stats(lat, wall):
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "small_p50_ms": float(np.percentile(lat[small], 50)) if small.any() else None,
+                "small_p99_ms": float(np.percentile(lat[small], 99)) if small.any() else None,
+                "req_per_s": n_req / wall, "ct_per_s": ct / wall}
+
     # capacity: every request submitted at once
-    reqs = make_reqs(n_req)
-    _, wall = run_server(reqs, np.zeros(n_req))
+    _, wall = run_server(np.zeros(n_req))
     capacity = n_req / wall
+    # service time of every request alone, one at a time (warmed up by the run above)
+    service = []
+    for q in reqs:
+        t = time.perf_counter()
+        plain_call(q)
+        service.append(time.perf_counter() - t)
+    service = np.array(service)
     out = {"capacity_req_per_s": capacity, "slots": slots, "budget_gb": budget / 2**30, "requests_per_level": n_req,
+           "small_requests": int(small.sum()), "plain_service_s_total": float(service.sum()),
+           "plain_method": "service time of each request measured alone; latencies at each load by the FIFO "
+                           "recursion over the level's arrival schedule (plain_live: the same loop run live)",
            "levels": []}
     for load in loads:
-        reqs = make_reqs(n_req)
-        ct = sum(q["n"] for q in reqs)
-        arrivals = np.cumsum(g.exponential(1.0 / (load * capacity), n_req))  # one schedule for both
-        ls, ws = run_server(reqs, arrivals)
-        lp, wp = run_plain(reqs, arrivals)
-        small = np.array([q["n"] <= SMALL_REQ for q in reqs])
-
-        def stats(lat, wall):
-            return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                    "small_p50_ms": float(np.percentile(lat[small], 50)) if small.any() else None,
-                    "small_p99_ms": float(np.percentile(lat[small], 99)) if small.any() else None,
-                    "req_per_s": n_req / wall, "ct_per_s": ct / wall}
-        out["levels"].append({"offered_load": load, "offered_req_per_s": load * capacity,
-                              "small_requests": int(small.sum()),
-                              "server": stats(ls, ws), "plain_per_request": stats(lp, wp)})
-        del reqs
+        arrivals = np.cumsum(g.exponential(1.0 / (load * capacity), n_req))
+        ls, ws = run_server(arrivals)
+        lp = fifo_latencies(arrivals, service) * 1e3
+        wp = max(arrivals[-1], 0.0) + lp[-1] / 1e3
+        lvl = {"offered_load": load, "offered_req_per_s": load * capacity,
+               "server": stats(ls, ws), "plain_per_request": stats(lp, wp)}
+        if load in live_plain:
+            ll, wl = run_plain(arrivals)
+            lvl["plain_live"] = stats(ll, wl)
+        out["levels"].append(lvl)
     return out
 
 
@@ -763,7 +921,8 @@ def run_ours(args):
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     sms = torch.cuda.get_device_properties(dist.local).multi_processor_count
-    imad = imad_peak(sms)
+    ip = int_peaks(sms, dist.local)
+    imad = ip["peak"] if ip else None
     h = headline(args, dist, ft, synth, torch, st)
     e = e2e(args, dist, ft, torch, h.pop("state"))
     achieved = W_ALG_SMUL * N_CT / (h["mul_ms"] * 1e-3)
@@ -785,7 +944,12 @@ def run_ours(args):
         "roofline": {"kernel": f"{kern} (CT variable-base ladder)", "bound": "int",
                      "achieved": achieved / 1e12, "peak": (imad or 0) / 1e12,
                      "unit": "T 32x32->64 mul-adds/s", "frac": (achieved / imad) if imad else None,
-                     "traffic": traffic, "peak_source": "measured IMAD.WIDE probe (libftbench.so)",
+                     "traffic": traffic,
+                     "peak_source": "measured integer probes (libftbench.so, csrc/bench_peak.cu): the higher of "
+                                    "mad.wide.u32 and mad.lo.u32 pairs, SM clock sampled during the probe",
+                     "peak_sm_mhz": ip and ip["sm_mhz"], "peak_per_sm_clk": ip and ip.get("per_sm_clk"),
+                     "probes_T": ip and {k: ip[k] / 1e12 for k in ("imad_wide", "imad_lo_pairs", "fe_mul")},
+                     "frac_of_fe_mul_probe": (achieved / ip["fe_mul"]) if ip and ip["fe_mul"] else None,
                      "algorithmic": f"{W_ALG_SMUL} products per scalar-mult x {N_CT} per launch",
                      "exact_products_per_smul": W_EXACT_SMUL,
                      "frac_exact": (W_EXACT_SMUL * N_CT / (h["mul_ms"] * 1e-3) / imad) if imad else None,
@@ -810,21 +974,23 @@ PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan",
                  "batch", "export")
 
 
-def run_profile(case: str) -> int:
+def run_profile(case: str, size: int | None = None) -> int:
     """One small run of one kernel family, for ncu (profiles/*.md): inputs are
     built, then the operation runs twice (the second launch is the one to
-    capture with `-s <setup launches + 1> -c 1` or `-k regex:<kernel>`)."""
+    capture with `-s <setup launches + 1> -c 1` or `-k regex:<kernel>`).
+    `size` (--profile-n) sets the number of points (ciphertext halves for
+    ct_add) in place of the case's default."""
     import torch
     import libftcrypto_gb300 as ft
     from libftcrypto_gb300 import synth
     ft.build()
     ft.init()
     g = synth.rng(SEED + 99)
-    n = 1 << 20
+    n = size or 1 << 20
     sc = synth.scalars_mod_L(g, n)
     d_sc = torch.from_numpy(sc).cuda()
     torch.cuda.synchronize()
-    base = ft.Array.from_scalars(sc[:4096])
+    base = ft.Array.from_scalars(sc[:min(n, 4096)])
     if case == "ladder":
         a = ft.Array.init_point(n, base, 1)
         op = lambda: a.mul_device(d_sc.data_ptr(), n)  # noqa: E731
@@ -837,7 +1003,7 @@ def run_profile(case: str) -> int:
     elif case == "comb":
         op = lambda: ft.Array.from_scalars(sc)  # noqa: E731
     elif case in ("add", "reduce", "scan", "segsum", "isum"):
-        big = 1 << 24 if case in ("reduce", "segsum") else 1 << 22
+        big = size or (1 << 24 if case in ("reduce", "segsum") else 1 << 22)
         a = ft.Array.init_point(big, base, 3)
         a.add(ft.Array.init_point(big, base, 5))
         if case == "add":
@@ -909,18 +1075,21 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--profile", choices=PROFILE_CASES, help="run one kernel family once, for ncu")
+    ap.add_argument("--profile-n", type=int, default=None, help="points of the --profile case")
     ap.add_argument("--serving-sweep", action="store_true",
                     help="only the serving sweep, offered load 10%%..100%% of capacity in 10%% steps")
+    ap.add_argument("--serving-requests", type=int, default=400, help="requests per level of the serving sweep")
     args = ap.parse_args()
     if args.profile:
-        return run_profile(args.profile)
+        return run_profile(args.profile, args.profile_n)
     if args.serving_sweep:
         import torch
         import libftcrypto_gb300 as ft
         from libftcrypto_gb300 import synth
         ft.build()
         ft.init()
-        res = serving(ft, synth, torch, loads=tuple(x / 10 for x in range(1, 11)), n_req=40)
+        res = serving(ft, synth, torch, loads=tuple(x / 10 for x in range(1, 11)), n_req=args.serving_requests,
+                      live_plain=())
         print(json.dumps({"serving_sweep": res}))
         return 0
     if args.impl == "reference":

@@ -63,6 +63,14 @@ ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint
  * ft_add(c2, d2) (or ft_sub), also when arrays alias (then it runs as those
  * two calls).  Arrays of one length. */
 ft_error ftx_ct_add(ft_ge25519_array c1, ft_ge25519_array c2, const_ft_ge25519_array d1, const_ft_ge25519_array d2);
+
+/* Ciphertext prefix scan: ft_array_scan (exclusive == 0) or
+ * ft_array_prescan (exclusive != 0) of c1 and of c2, both halves through the
+ * same launches, so they share the scan's latency-bound lower levels
+ * (ft_array_scan / ft_array_prescan, ftcrypto.cu:1474-1586, applied to each
+ * half of a ciphertext array).  Arrays of one length; the same array passed
+ * twice is scanned twice. */
+ft_error ftx_ct_scan(ft_ge25519_array c1, ft_ge25519_array c2, int exclusive);
 ft_error ftx_ct_sub(ft_ge25519_array c1, ft_ge25519_array c2, const_ft_ge25519_array d1, const_ft_ge25519_array d2);
 
 /* Re-randomisation: (c1_i, c2_i) += (r_i * B, r_i * pk), a fresh encryption
@@ -149,8 +157,12 @@ void ftx_batch_free(ftx_batch batch);
  * the express slots first and may overtake queued large requests.  Admitted
  * requests run concurrently, so work of requests arriving while others are
  * on the GPU overlaps with theirs.  Ciphertexts stay on the device as handles: ENCRYPT and SEGSUM
- * create new arrays (the caller frees them with ft_array_free), RERAND and
- * SMUL update the given arrays in place.  Host buffers named in a request
+ * create new arrays, RERAND and SMUL update the given arrays in place.  The
+ * budget counts a request's temporaries while it runs and the arrays it
+ * creates until the caller hands them back with ftx_server_release (which
+ * frees them): outputs kept resident hold their share of the budget, and
+ * requests wait for it (freeing such an array with ft_array_free while the
+ * server lives leaves its bytes charged).  Host buffers named in a request
  * must stay valid until its result is returned; arrays of a request must not
  * be used elsewhere until then.  Results are bit-identical to the same
  * request run alone. */
@@ -182,9 +194,15 @@ ft_error ftx_server_create(ftx_server *server, const uint8_t *pk, size_t hbm_bud
 ft_error ftx_server_submit(ftx_server server, const ftx_request *req, uint64_t *ticket);
 /* blocks until the request completes */
 ft_error ftx_server_wait(ftx_server server, uint64_t ticket, ftx_result *result);
-/* bytes of the budget in use and requests queued / running */
+/* frees an array that a request of this server created (a result's c1 or
+ * c2) and returns its bytes to the budget; FT_ERR_OUT_OF_BOUNDS for an array
+ * the server does not hold (not its output, or already released) */
+ft_error ftx_server_release(ftx_server server, ft_ge25519_array array);
+/* bytes of the budget in use (running requests, and outputs not yet
+ * released) and requests queued / running */
 ft_error ftx_server_stats(ftx_server server, size_t *bytes_in_use, size_t *queued, size_t *running);
-/* waits for every request; frees the new arrays of results never collected */
+/* waits for every request; frees the new arrays of results never collected
+ * (collected, unreleased outputs stay valid; the caller frees them) */
 void ftx_server_free(ftx_server server);
 
 /* Launch-shape knobs, set by the autotuner (libftcrypto_gb300/autotune.py)
@@ -209,7 +227,9 @@ int ftx_tune_get(int knob);
  * GPU that loads it.  n <= FT_NOALLOC_SCAN_MAX_POINTS (FT_ERR_BAD_SIZE
  * otherwise).  All calls share that array: calls that overlap on the GPU
  * race and must be serialised.  The first call on a device looks up the
- * array's address; make it before any stream capture. */
+ * array's address and keeps it for the life of the process; make it before
+ * any stream capture.  A cudaDeviceReset of that device is not supported
+ * afterwards (the array may move when the module is loaded again). */
 #define FT_NOALLOC_SCAN_MAX_POINTS 1048576
 ft_error ftx_scan_noalloc(void *d_planes, size_t stride, size_t n, int exclusive, void *stream);
 

@@ -1,8 +1,8 @@
 """ctypes binding of libftcrypto.so (include/ftcrypto.h + include/ftcrypto_gb300.h).
 
 Loading fails loudly when the compiled library is missing: there is no
-fallback implementation.  This module is also the reference-side binding a
-Python caller of the reference library would write.
+fallback implementation.  This module is also the binding a Python caller
+of the reference library would write against the same header.
 """
 from __future__ import annotations
 
@@ -72,6 +72,7 @@ SIGNATURES = {
     "ftx_encrypt": (I, [PP, PP, P, P, P, S, U]),
     "ftx_encrypt_device": (I, [P, P, P, P, P, S, U]),
     "ftx_ct_add": (I, [P, P, P, P]),
+    "ftx_ct_scan": (I, [P, P, I]),
     "ftx_ct_sub": (I, [P, P, P, P]),
     "ftx_rerandomise": (I, [P, P, P, P, S]),
     "ftx_rerandomise_device": (I, [P, P, P, P, S]),
@@ -112,6 +113,7 @@ SIGNATURES.update({
     "ftx_server_create": (I, [PP, P, S, I]),
     "ftx_server_submit": (I, [P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
     "ftx_server_wait": (I, [P, ctypes.c_uint64, ctypes.POINTER(Result)]),
+    "ftx_server_release": (I, [P, P]),
     "ftx_server_stats": (I, [P, PS, PS, PS]),
     "ftx_server_free": (None, [P]),
 })

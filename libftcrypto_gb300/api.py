@@ -304,6 +304,11 @@ def ct_add(c1: Array, c2: Array, d1: Array, d2: Array) -> None:
     check(lib().ftx_ct_add(c1.handle, c2.handle, d1.handle, d2.handle))
 
 
+def ct_scan(c1: Array, c2: Array, exclusive: bool = False) -> None:
+    """Prefix scan of both halves of a ciphertext array in one call."""
+    check(lib().ftx_ct_scan(c1.handle, c2.handle, 1 if exclusive else 0))
+
+
 def ct_sub(c1: Array, c2: Array, d1: Array, d2: Array) -> None:
     check(lib().ftx_ct_sub(c1.handle, c2.handle, d1.handle, d2.handle))
 
@@ -399,9 +404,41 @@ TUNE_BATCH_ADD_PTS = 2
 REQ_ENCRYPT, REQ_RERAND, REQ_SMUL, REQ_SEGSUM = 1, 2, 3, 4
 
 
+class ServerArray(Array):
+    """An output array a Server holds against its budget: free() (or garbage
+    collection) hands it back through ftx_server_release while the server
+    lives, and frees it as a plain array after the server is closed."""
+
+    __slots__ = ("_srv",)
+
+    def __init__(self, handle: ctypes.c_void_p, server: "Server"):
+        super().__init__(handle)
+        self._srv = server
+
+    def free(self) -> None:
+        if self._h:
+            srv, self._srv = self._srv, None
+            h, self._h = self._h, None
+            if srv is not None and srv._h:
+                check(lib().ftx_server_release(srv._h, h))
+            else:
+                lib().ft_array_free(h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            srv = getattr(self, "_srv", None)
+            if srv is not None and srv._h:
+                _lib._lib.ftx_server_release(srv._h, self._h)
+            else:
+                _lib._lib.ft_array_free(self._h)
+            self._h = None
+
+
 class Server:
     """ftx_server: continuous-batching request loop (see ftcrypto_gb300.h).
-    Host buffers of a request are kept alive until its result is taken."""
+    Host buffers of a request are kept alive until its result is taken.
+    Arrays a request creates are ServerArray objects charged to the budget
+    until freed (release())."""
 
     def __init__(self, pk32, hbm_budget_bytes: int, slots: int = 8):
         pk = _buf(pk32, np.uint8).reshape(32)
@@ -447,8 +484,13 @@ class Server:
         if in_place is not None:
             c1, c2 = in_place
         else:
-            c1, c2 = Array(ctypes.c_void_p(res.c1)), Array(ctypes.c_void_p(res.c2))
+            c1, c2 = ServerArray(ctypes.c_void_p(res.c1), self), ServerArray(ctypes.c_void_p(res.c2), self)
         return c1, c2, res.queue_ms, res.latency_ms
+
+    def release(self, *arrays: ServerArray) -> None:
+        """Hand outputs back: frees them and returns their bytes to the budget."""
+        for a in arrays:
+            a.free()
 
     def stats(self):
         a, b, c = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()

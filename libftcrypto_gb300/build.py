@@ -72,7 +72,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     subprocess.check_call([cc] + ARCH + ["-shared", "-o", tmp] + objs)
     os.replace(tmp, LIB)
     bench_src = os.path.join(CSRC, "bench_peak.cu")
-    if force or not os.path.exists(BENCH_LIB) or os.path.getmtime(BENCH_LIB) < os.path.getmtime(bench_src):
+    bench_deps = [bench_src] + [os.path.join(CSRC, f) for f in ("fe.cuh", "ptx.cuh")]
+    if force or not os.path.exists(BENCH_LIB) or os.path.getmtime(BENCH_LIB) < max(map(os.path.getmtime, bench_deps)):
         subprocess.check_call([cc] + FLAGS + ["-shared", "-o", BENCH_LIB, bench_src])
     return LIB
 

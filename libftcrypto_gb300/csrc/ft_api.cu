@@ -785,16 +785,30 @@ ft_error ft_reduce_isum(ft_ge25519_array res, const size_t *idxs, size_t n, cons
     size_t b_sort = align256(ft::isum_scratch_bytes(n, nk));
     size_t b_seg = align256(ft::segsum_scratch_bytes(n));
     void *s;
-    CK(scratch(&s, b_keys + b_off + b_perm + b_sort + b_seg));
+    CK(scratch(&s, b_keys + b_off + b_perm + b_sort + b_seg + 256));
     uint8_t *base = (uint8_t *)s;
     uint64_t *keys = (uint64_t *)base;
     int32_t *off = (int32_t *)(base + b_keys);
     int32_t *perm = (int32_t *)(base + b_keys + b_off);
     void *sort_tmp = base + b_keys + b_off + b_perm;
+    void *seg_tmp = base + b_keys + b_off + b_perm + b_sort;
+    int32_t *d_maxlen = (int32_t *)(base + b_keys + b_off + b_perm + b_sort + b_seg);
     CK(h2d(keys, idxs, n * 8));
     if ((err = status_reset())) return err;
     CK(ft::keys_to_csr(off, perm, keys, n, nk, g.d_status, sort_tmp, g.stream));
-    void *seg_tmp = base + b_keys + b_off + b_perm + b_sort;
+    // a key repeated thousands of times is a long segment: sum those layouts
+    // through a scan (one wait for the largest count decides)
+    int32_t maxlen = 0;
+    CK(ft::segment_maxlen(off, nk, d_maxlen, g.stream));
+    CK(d2h(&maxlen, d_maxlen, sizeof maxlen));
+    if (ft::segsum_prefers_prefix(n, (size_t)maxlen)) {
+        void *t = nullptr;
+        CK(dev_alloc(&t, ft::segsum_prefix_scratch_bytes(n)));
+        cudaError_t e = ft::segsum_prefix(ft::view_of(res), off, nk, ft::view_of(src), n, perm, 1, t, g.stream);
+        dev_free(t);
+        CK(e);
+        return FT_ERR_NO_ERROR;
+    }
     CK(ft::segsum(ft::view_of(res), off, nk, ft::view_of(src), n, perm, 1, seg_tmp, g.stream));
     return FT_ERR_NO_ERROR;
 }
@@ -884,6 +898,23 @@ static ft_error scan_impl(ft_ge25519_array array, int exclusive)
 
 ft_error ft_array_prescan(ft_ge25519_array array) { return scan_impl(array, 1); }
 ft_error ft_array_scan(ft_ge25519_array array) { return scan_impl(array, 0); }
+
+ft_error ftx_ct_scan(ft_ge25519_array c1, ft_ge25519_array c2, int exclusive)
+{
+    ENSURE_INIT();
+    if (c1->n != c2->n) return FT_ERR_SIZE_MISMATCH;
+    if (c1 == c2) { // the same array twice: the two ft_array_scan calls it stands for
+        ft_error err = scan_impl(c1, exclusive ? 1 : 0);
+        return err ? err : scan_impl(c2, exclusive ? 1 : 0);
+    }
+    size_t n = c1->n;
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    CK(scratch(&s, ft::scan_scratch_bytes(n, 2)));
+    const ft::View v[2] = {ft::view_of(c1), ft::view_of(c2)};
+    CK(ft::scan_set(v, 2, n, exclusive ? 1 : 0, s, g.stream));
+    return FT_ERR_NO_ERROR;
+}
 
 ft_error ft_array_reduce(ft_ge25519_array array)
 {
@@ -1124,16 +1155,26 @@ ft_error ftx_segmented_sum_csr(ft_ge25519_array *out, const int32_t *off, size_t
     ENSURE_INIT();
     if (src->n >= (size_t)INT32_MAX || nseg >= (size_t)INT32_MAX) return FT_ERR_BAD_SIZE;
     if (off[0] != 0 || (size_t)off[nseg] != src->n) return FT_ERR_BAD_SIZE;
-    for (size_t s = 0; s < nseg; ++s)
+    size_t maxlen = 0;
+    for (size_t s = 0; s < nseg; ++s) {
         if (off[s + 1] < off[s]) return FT_ERR_BAD_SIZE;
+        maxlen = std::max(maxlen, (size_t)(off[s + 1] - off[s]));
+    }
+    // long segments go through a scan: the walk's join would add their
+    // thread parts one after another
+    const bool prefix = ft::segsum_prefers_prefix(src->n, maxlen);
     return with_new_array(out, nseg, [&](ft_ge25519_array a) -> ft_error {
         if (nseg == 0) return FT_ERR_NO_ERROR;
         void *s;
         size_t b_off = align256((nseg + 1) * 4);
-        CK(scratch(&s, b_off + ft::segsum_scratch_bytes(src->n)));
+        CK(scratch(&s, b_off + (prefix ? ft::segsum_prefix_scratch_bytes(src->n) : ft::segsum_scratch_bytes(src->n))));
         CK(h2d(s, off, (nseg + 1) * 4));
-        CK(ft::segsum(ft::view_of(a), (const int32_t *)s, nseg, ft::view_of(src), src->n, nullptr, 0,
-                      (uint8_t *)s + b_off, g.stream));
+        if (prefix)
+            CK(ft::segsum_prefix(ft::view_of(a), (const int32_t *)s, nseg, ft::view_of(src), src->n, nullptr, 0,
+                                 (uint8_t *)s + b_off, g.stream));
+        else
+            CK(ft::segsum(ft::view_of(a), (const int32_t *)s, nseg, ft::view_of(src), src->n, nullptr, 0,
+                          (uint8_t *)s + b_off, g.stream));
         return FT_ERR_NO_ERROR;
     });
 }

@@ -128,12 +128,23 @@ constexpr size_t scan_scratch_points(size_t n)
                                : (n + scan_level_k(n) - 1) / scan_level_k(n) +
                                      scan_scratch_points((n + scan_level_k(n) - 1) / scan_level_k(n));
 }
-size_t scan_scratch_bytes(size_t n);
+size_t scan_scratch_bytes(size_t n, int m = 1);
 cudaError_t scan(View v, size_t n, int exclusive, void *d_scratch, cudaStream_t st);
+// m (1 or 2) arrays of n points each scanned by the same launches
+cudaError_t scan_set(const View *v, int m, size_t n, int exclusive, void *d_scratch, cudaStream_t st);
 // out[s] (+)= sum of src[perm ? perm[e] : e] for e in [off[s], off[s+1])
 size_t segsum_scratch_bytes(size_t nsrc);
 cudaError_t segsum(View out, const int32_t *d_off, size_t nseg, View src, size_t nsrc,
                    const int32_t *d_perm, int accumulate, void *d_scratch, cudaStream_t st);
+// the same sums as segsum through one inclusive scan of the (gathered) points
+// and a difference of two prefixes per segment: for layouts with long
+// segments, which the walk's join adds up one thread part after another
+bool segsum_prefers_prefix(size_t nsrc, size_t max_len);
+size_t segsum_prefix_scratch_bytes(size_t nsrc);
+cudaError_t segsum_prefix(View out, const int32_t *d_off, size_t nseg, View src, size_t nsrc,
+                          const int32_t *d_perm, int accumulate, void *d_scratch, cudaStream_t st);
+// *d_max = the largest segment length of a CSR layout
+cudaError_t segment_maxlen(const int32_t *d_off, size_t nseg, int32_t *d_max, cudaStream_t st);
 // counting sort of keys < nkeys: d_off (nkeys + 1) and d_perm (n); *d_bad set to
 // the largest out-of-range position, or left at -1
 size_t isum_scratch_bytes(size_t n, size_t nkeys);

@@ -19,7 +19,10 @@
 //    host threads) race on the array and give wrong results: serialise them.
 //  * the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    before any stream capture.  The address is kept for the life of the
+//    process: after a cudaDeviceReset the module is loaded again and the
+//    array may lie elsewhere, so calling this entry point on a device that
+//    was reset is not supported.
 #include <mutex>
 
 #include "internal.h"
@@ -38,7 +41,8 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void *g_addr[kMaxDevices];
 
-// device address of the scratch array on the current device (once per device)
+// device address of the scratch array on the current device, looked up once
+// per device and kept (a cudaDeviceReset afterwards is not supported)
 cudaError_t scratch_address(void **out)
 {
     int dev = 0;

@@ -135,10 +135,43 @@ FT_DEV void block_scan_excl(ge_p3 &ex, const ge_p3 &x, uint4 *sm /* (NT/32) * 8 
     ge_addto(ex, lex);
 }
 
+// The scan kernels take up to two arrays of one length (the two halves of a
+// ciphertext array, ftx_ct_scan): blockIdx.y selects the array, so both are
+// scanned by the same launches and share the latency-bound lower levels.
+struct ScanSet {
+    uint4 *p[2];
+    size_t s[2];
+    // array blockIdx.y, chosen by selects (indexing the parameter array with
+    // blockIdx.y would copy it to local memory)
+    FT_DEV uint4 *ptr() const { return blockIdx.y ? p[1] : p[0]; }
+    FT_DEV size_t stride() const { return blockIdx.y ? s[1] : s[0]; }
+};
+
+// blocks per SM the scan's and the segmented sum's walks are compiled for
+// (__launch_bounds__ minimum; 1 leaves the register count to ptxas).
+// Measured on GB300 for the 2 x 4,194,304-point ciphertext scan: 1.95 ms
+// unconstrained (sums ~152 registers, apply ~184), 2.09 ms at 3 blocks,
+// 2.11 ms at 4 for the sums and 3 for the rescan, 2.68 ms at 4 for both
+// (128 registers, spills); the segmented-sum walk 1.73 ms at 4 blocks
+// (128 registers) against 1.81 ms at 3.
+#ifndef FT_SCAN_SUMS_MINB
+#define FT_SCAN_SUMS_MINB 1
+#endif
+#ifndef FT_SCAN_APPLY_MINB
+#define FT_SCAN_APPLY_MINB 1
+#endif
+#ifndef FT_SEG_WALK_MINB
+#define FT_SEG_WALK_MINB 4
+#endif
+
 // per-thread sums of K consecutive points: ts[t] = sum of p[tK .. tK+K)
 template <int K>
-__global__ void __launch_bounds__(128) k_scan_sums(const uint4 *p, size_t s, size_t n, uint4 *ts, size_t tss)
+__global__ void __launch_bounds__(128, FT_SCAN_SUMS_MINB) k_scan_sums(ScanSet in, size_t n, ScanSet ts)
 {
+    const uint4 *p = in.ptr();
+    const size_t s = in.stride();
+    uint4 *tp = ts.ptr();
+    const size_t tss = ts.stride();
     const size_t nt = (n + K - 1) / K;
     FT_GRID_LOOP(t, nt)
     {
@@ -153,20 +186,23 @@ __global__ void __launch_bounds__(128) k_scan_sums(const uint4 *p, size_t s, siz
             ld_p3(x, p, s, e);
             ge_addto(acc, x);
         }
-        st_p3(ts, tss, t, acc);
+        st_p3(tp, tss, t, acc);
     }
 }
 
 // rescan each thread's K points starting from its exclusive prefix ts[t]
 template <int K>
-__global__ void __launch_bounds__(128) k_scan_apply(uint4 *p, size_t s, size_t n, const uint4 *ts, size_t tss,
-                                                    int exclusive)
+__global__ void __launch_bounds__(128, FT_SCAN_APPLY_MINB) k_scan_apply(ScanSet io, size_t n, ScanSet ts, int exclusive)
 {
+    uint4 *p = io.ptr();
+    const size_t s = io.stride();
+    const uint4 *tp = ts.ptr();
+    const size_t tss = ts.stride();
     const size_t nt = (n + K - 1) / K;
     FT_GRID_LOOP(t, nt)
     {
         ge_p3 pre;
-        ld_p3(pre, ts, tss, t);
+        ld_p3(pre, tp, tss, t);
 #pragma unroll 1
         for (int k = 0; k < K; ++k) {
             const size_t e = t * K + k;
@@ -180,16 +216,18 @@ __global__ void __launch_bounds__(128) k_scan_apply(uint4 *p, size_t s, size_t n
     }
 }
 
-// one block scans n <= NT * kpt points in place: sums of kpt consecutive
-// points per thread, a block-wide exclusive scan of them, then the
-// sequential rescan.  One block is latency-bound, so the points are spread
-// over all NT threads (kpt = ceil(n / NT)): the last level of a 4M-point scan
-// (1,024 points) is a chain of 17 dependent additions instead of 41 with a
-// fixed 16 points per thread (194 us per launch).
+// one block per array scans n <= NT * kpt points in place: sums of kpt
+// consecutive points per thread, a block-wide exclusive scan of them, then
+// the sequential rescan.  One block is latency-bound, so the points are
+// spread over all NT threads (kpt = ceil(n / NT)): the last level of a
+// 4M-point scan (1,024 points) is a chain of 17 dependent additions instead
+// of 41 with a fixed 16 points per thread (194 us per launch).
 template <int NT>
-__global__ void __launch_bounds__(NT) k_scan_small(uint4 *p, size_t s, size_t n, int kpt, int exclusive)
+__global__ void __launch_bounds__(NT) k_scan_small(ScanSet io, size_t n, int kpt, int exclusive)
 {
     __shared__ uint4 sm[(NT / 32) * 8];
+    uint4 *p = io.ptr();
+    const size_t s = io.stride();
     const size_t e0 = (size_t)threadIdx.x * kpt;
     ge_p3 acc;
     ge_p3_0(acc);
@@ -218,35 +256,53 @@ __global__ void __launch_bounds__(NT) k_scan_small(uint4 *p, size_t s, size_t n,
 
 static const int SMALL_NT = 256;
 
-size_t scan_scratch_bytes(size_t n) { return scan_scratch_points(n) * 128 + 256; }
+size_t scan_scratch_bytes(size_t n, int m) { return (size_t)m * scan_scratch_points(n) * 128 + 256; }
 
 // thread sums of K = scan_level_k(n) points, an exclusive scan of those sums
-// (the same routine on an array K times shorter, until one block suffices),
+// (the same routine on arrays K times shorter, until one block suffices),
 // then the rescan: about 2 + 2/K additions per point, no waits between blocks.
 // At 4M points the lower levels (262,144 points down to 4,096) take 4 points
 // per thread: 16 made each of their launches a 16-addition chain in
-// under-filled waves (~60 us each).
-cudaError_t scan(View v, size_t n, int exclusive, void *scratch, cudaStream_t st)
+// under-filled waves (~60 us each).  m arrays (1 or 2) of n points each go
+// through the same launches; scratch holds m x scan_scratch_points(n) points.
+cudaError_t scan_set(const View *v, int m, size_t n, int exclusive, void *scratch, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
+    if (m < 1 || m > 2) return cudaErrorInvalidValue;
+    ScanSet io{};
+    for (int i = 0; i < m; ++i) {
+        io.p[i] = v[i].p;
+        io.s[i] = v[i].s;
+    }
     if (n <= SCAN_SMALL_MAX) {
         const int kpt = (int)((n + SMALL_NT - 1) / SMALL_NT);
-        k_scan_small<SMALL_NT><<<1, SMALL_NT, 0, st>>>(v.p, v.s, n, kpt, exclusive);
+        k_scan_small<SMALL_NT><<<dim3(1, m), SMALL_NT, 0, st>>>(io, n, kpt, exclusive);
         return cudaGetLastError();
     }
     const size_t K = scan_level_k(n);
     const size_t nt = (n + K - 1) / K;
-    View ts{(uint4 *)scratch, nt};
-    void *rest = ts.p + FT_PLANES * nt;
-    const unsigned grid = (unsigned)((nt + 127) / 128);
-    if (K == 16) k_scan_sums<16><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s);
-    else k_scan_sums<4><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s);
+    View ts[2];
+    ScanSet tset{};
+    for (int i = 0; i < m; ++i) {
+        ts[i] = View{(uint4 *)scratch + (size_t)i * FT_PLANES * nt, nt};
+        tset.p[i] = ts[i].p;
+        tset.s[i] = nt;
+    }
+    void *rest = (uint4 *)scratch + (size_t)m * FT_PLANES * nt;
+    const dim3 grid((unsigned)((nt + 127) / 128), m);
+    if (K == 16) k_scan_sums<16><<<grid, 128, 0, st>>>(io, n, tset);
+    else k_scan_sums<4><<<grid, 128, 0, st>>>(io, n, tset);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    if ((e = scan(ts, nt, 1, rest, st)) != cudaSuccess) return e;
-    if (K == 16) k_scan_apply<16><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s, exclusive);
-    else k_scan_apply<4><<<grid, 128, 0, st>>>(v.p, v.s, n, ts.p, ts.s, exclusive);
+    if ((e = scan_set(ts, m, nt, 1, rest, st)) != cudaSuccess) return e;
+    if (K == 16) k_scan_apply<16><<<grid, 128, 0, st>>>(io, n, tset, exclusive);
+    else k_scan_apply<4><<<grid, 128, 0, st>>>(io, n, tset, exclusive);
     return cudaGetLastError();
+}
+
+cudaError_t scan(View v, size_t n, int exclusive, void *scratch, cudaStream_t st)
+{
+    return scan_set(&v, 1, n, exclusive, scratch, st);
 }
 
 // ------------------------------------------------------------ reduce launcher
@@ -313,7 +369,7 @@ FT_DEV void seg_write(uint4 *op, size_t os, int sg, const ge_p3 &v, int accumula
 // four blocks per SM (128 registers, a few spills to L1) rather than two at
 // 202 registers: 2.58 against 2.68 ms for 16,777,216 points (measured)
 template <int K>
-__global__ void __launch_bounds__(128, 4) k_seg_walk(uint4 *op, size_t os, const int32_t *off, int nseg, const uint4 *sp,
+__global__ void __launch_bounds__(128, FT_SEG_WALK_MINB) k_seg_walk(uint4 *op, size_t os, const int32_t *off, int nseg, const uint4 *sp,
                                                   size_t ss, long long nsrc, const int32_t *perm, int accumulate,
                                                   uint4 *H, uint4 *Lp, size_t hs, uint32_t *flags, int32_t *lseg)
 {
@@ -438,24 +494,129 @@ cudaError_t segsum(View out, const int32_t *off, size_t nseg, View src, size_t n
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------ long segments
+
+// dst[e] = src[perm[e]]
+__global__ void __launch_bounds__(256) k_gather_i32(uint4 *d, size_t ds, const uint4 *s, size_t ss,
+                                                    const int32_t *perm, size_t n)
+{
+    FT_GRID_LOOP(e, n)
+    {
+        const size_t j = (size_t)perm[e];
+#pragma unroll
+        for (int k = 0; k < FT_PLANES; ++k) d[k * ds + e] = s[k * ss + j];
+    }
+}
+
+// out[s] (+)= P[off[s+1] - 1] - P[off[s] - 1], P the inclusive prefix sums
+// (P[-1] the identity): each segment as a difference of two prefixes
+__global__ void __launch_bounds__(128) k_seg_diff(uint4 *op, size_t os, const int32_t *off, size_t nseg,
+                                                  const uint4 *P, size_t ps, int accumulate)
+{
+    FT_GRID_LOOP(sg, nseg)
+    {
+        const int32_t a = off[sg], b = off[sg + 1];
+        ge_p3 v;
+        if (a == b) {
+            if (accumulate) continue;
+            ge_p3_0(v);
+        } else {
+            ld_p3(v, P, ps, (size_t)b - 1);
+            if (a > 0) {
+                ge_p3 q;
+                ld_p3(q, P, ps, (size_t)a - 1);
+                ge_subfrom(v, q);
+            }
+        }
+        seg_write(op, os, (int)sg, v, accumulate);
+    }
+}
+
+// the largest off[s+1] - off[s] into *d_max (which the caller zeroes)
+__global__ void __launch_bounds__(256) k_seg_maxlen(const int32_t *off, size_t nseg, int32_t *d_max)
+{
+    int32_t m = 0;
+    FT_GRID_LOOP(sg, nseg) m = max(m, off[sg + 1] - off[sg]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(d_max, m);
+}
+
+cudaError_t segment_maxlen(const int32_t *d_off, size_t nseg, int32_t *d_max, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(d_max, 0, sizeof(int32_t), st);
+    if (e != cudaSuccess || nseg == 0) return e;
+    k_seg_maxlen<<<(unsigned)std::min<size_t>((nseg + 255) / 256, 1024), 256, 0, st>>>(d_off, nseg, d_max);
+    return cudaGetLastError();
+}
+
+bool segsum_prefers_prefix(size_t nsrc, size_t max_len)
+{
+    // the walk's join adds the parts of a segment spanning m threads one
+    // after another (m = length / 32, ~7 us each); the prefix path costs
+    // about one scan more than the walk, whatever the lengths
+    return max_len > std::max<size_t>(2048, nsrc / 1024);
+}
+
+size_t segsum_prefix_scratch_bytes(size_t nsrc)
+{
+    return ((nsrc * 128 + 255) / 256) * 256 + scan_scratch_bytes(nsrc);
+}
+
+// the same sums through one inclusive scan of the (gathered) points and a
+// difference of two prefixes per segment: ~2 additions per point, and no
+// chain of additions longer than the scan's whatever the segment lengths
+cudaError_t segsum_prefix(View out, const int32_t *off, size_t nseg, View src, size_t nsrc, const int32_t *perm,
+                          int accumulate, void *scratch, cudaStream_t st)
+{
+    if (nseg == 0) return cudaSuccess;
+    View P{(uint4 *)scratch, nsrc};
+    void *scan_tmp = (uint8_t *)scratch + ((nsrc * 128 + 255) / 256) * 256;
+    cudaError_t e = cudaSuccess;
+    if (nsrc) {
+        if (perm) {
+            k_gather_i32<<<(unsigned)std::min<size_t>((nsrc + 255) / 256, (size_t)sm_count() * 16), 256, 0, st>>>(
+                P.p, P.s, src.p, src.s, perm, nsrc);
+            e = cudaGetLastError();
+        } else {
+            e = copy_points(P, src, nsrc, st);
+        }
+        if (e == cudaSuccess) e = scan(P, nsrc, 0, scan_tmp, st);
+        if (e != cudaSuccess) return e;
+    }
+    k_seg_diff<<<(unsigned)std::min<size_t>((nseg + 127) / 128, (size_t)sm_count() * 32), 128, 0, st>>>(
+        out.p, out.s, off, nseg, P.p, P.s, accumulate);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ counting sort
 
+// Lanes of a warp holding the same key add their count with one atomic (the
+// lowest of them): repeated keys, up to all keys equal, do not serialise on
+// one counter.
 __global__ void k_key_hist(const uint64_t *keys, size_t n, size_t nkeys, int32_t *cnt, long long *bad)
 {
     FT_GRID_LOOP(i, n)
     {
-        uint64_t k = keys[i];
+        const uint64_t k = keys[i];
+        const unsigned peers = __match_any_sync(__activemask(), k);
         if (k >= nkeys) atomicMax(bad, (long long)i);
-        else atomicAdd(&cnt[k], 1);
+        else if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&cnt[k], __popc(peers));
     }
 }
 
+// places index i of key k at cur[k] + its rank among the warp's lanes of key k
 __global__ void k_key_place(const uint64_t *keys, size_t n, size_t nkeys, int32_t *cur, int32_t *perm)
 {
     FT_GRID_LOOP(i, n)
     {
-        uint64_t k = keys[i];
-        if (k < nkeys) perm[atomicAdd(&cur[k], 1)] = (int32_t)i;
+        const uint64_t k = keys[i];
+        const unsigned peers = __match_any_sync(__activemask(), k);
+        const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+        int32_t base = 0;
+        if (k < nkeys && lane == leader) base = atomicAdd(&cur[k], __popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        if (k < nkeys) perm[base + __popc(peers & ((1u << lane) - 1u))] = (int32_t)i;
     }
 }
 

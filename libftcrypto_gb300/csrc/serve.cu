@@ -19,6 +19,13 @@
 // blocks are dispatched as soon as SMs free up.  Admission is FIFO within
 // each class; an express request may overtake queued bulk requests (the
 // requests of a server touch disjoint arrays, so order does not matter).
+//
+// Budget: a request is charged its temporaries (staged inputs, scratch)
+// while it runs and the arrays it creates (ENCRYPT, SEGSUM outputs) from
+// admission until the caller hands them back with ftx_server_release, so
+// the budget bounds what the server keeps resident, not only what is in
+// flight.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -43,11 +50,13 @@ using Clock = std::chrono::steady_clock;
 struct Req {
     ftx_request r;
     uint64_t ticket = 0;
-    size_t bytes = 0;
+    size_t bytes = 0;     // temporaries, charged while the request runs
+    size_t out_bytes = 0; // arrays it creates, charged until released
     Clock::time_point t_submit, t_admit, t_done;
     ftx_result res{};
     int slot = -1;
     bool express = false;   // small enough for the high-priority slots
+    bool seg_prefix = false; // SEGSUM with long segments: summed through a scan
     bool done = false;      // set by the stream callback
     bool finished = false;  // result published
     std::vector<void *> tmp;
@@ -75,14 +84,27 @@ double request_cost(const ftx_request &r)
     }
 }
 
-size_t request_bytes(const ftx_request &r)
+// device bytes of the arrays a request creates (its two output arrays)
+size_t request_out_bytes(const ftx_request &r)
 {
     const size_t pts = FT_PLANES_BYTES_PER_POINT;
     switch (r.op) {
-    case FTX_REQ_ENCRYPT: return 2 * r.n * pts + r.n * 40 + 4096;
+    case FTX_REQ_ENCRYPT: return 2 * r.n * pts;
+    case FTX_REQ_SEGSUM: return 2 * r.nseg * pts;
+    default: return 0;
+    }
+}
+
+// device bytes a request takes only while it runs (staged inputs, scratch)
+size_t request_tmp_bytes(const ftx_request &r, bool seg_prefix)
+{
+    switch (r.op) {
+    case FTX_REQ_ENCRYPT: return r.n * 40 + 4096;
     case FTX_REQ_RERAND: return r.n * 32 + 4096;
     case FTX_REQ_SMUL: return r.n * 32 + 4096;
-    case FTX_REQ_SEGSUM: return 2 * r.nseg * pts + (r.nseg + 1) * 4 + 2 * ft::segsum_scratch_bytes(r.n) + 8192;
+    case FTX_REQ_SEGSUM:
+        return (r.nseg + 1) * 4 + 8192 +
+               2 * (seg_prefix ? ft::segsum_prefix_scratch_bytes(r.n) : ft::segsum_scratch_bytes(r.n));
     default: return 0;
     }
 }
@@ -95,7 +117,10 @@ struct ftx_server_s {
     std::list<Req *> pending; // iterators stay valid while submitters append
     std::map<uint64_t, Req *> reqs;
     std::vector<Slot> slots;
-    size_t budget = 0, in_use = 0, running = 0;
+    // in_use: temporaries and outputs of running requests; resident: outputs
+    // of finished requests not yet released (held maps each to its bytes)
+    size_t budget = 0, in_use = 0, resident = 0, running = 0;
+    std::map<ft_ge25519_array, size_t> held;
     uint64_t next_ticket = 1;
     bool stop = false;
     uint32_t *pk_table = nullptr;
@@ -202,15 +227,15 @@ ft_error ftx_server_s::dispatch(Req *q, Slot &sl)
         e = new_array(&q->res.c1, r.nseg, st);
         if (e == cudaSuccess) e = new_array(&q->res.c2, r.nseg, st);
         if (e == cudaSuccess) e = alloc_on(q, &doff, (r.nseg + 1) * 4, st);
-        if (e == cudaSuccess) e = alloc_on(q, &s1, ft::segsum_scratch_bytes(r.n), st);
-        if (e == cudaSuccess) e = alloc_on(q, &s2, ft::segsum_scratch_bytes(r.n), st);
+        const size_t sb = q->seg_prefix ? ft::segsum_prefix_scratch_bytes(r.n) : ft::segsum_scratch_bytes(r.n);
+        auto sum = q->seg_prefix ? ft::segsum_prefix : ft::segsum;
+        if (e == cudaSuccess) e = alloc_on(q, &s1, sb, st);
+        if (e == cudaSuccess) e = alloc_on(q, &s2, sb, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(doff, r.offsets, (r.nseg + 1) * 4, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess)
-            e = ft::segsum(ft::view_of(q->res.c1), (const int32_t *)doff, r.nseg, ft::view_of(r.c1), r.n, nullptr, 0,
-                           s1, st);
+            e = sum(ft::view_of(q->res.c1), (const int32_t *)doff, r.nseg, ft::view_of(r.c1), r.n, nullptr, 0, s1, st);
         if (e == cudaSuccess)
-            e = ft::segsum(ft::view_of(q->res.c2), (const int32_t *)doff, r.nseg, ft::view_of(r.c2), r.n, nullptr, 0,
-                           s2, st);
+            e = sum(ft::view_of(q->res.c2), (const int32_t *)doff, r.nseg, ft::view_of(r.c2), r.n, nullptr, 0, s2, st);
         break;
     }
     default: return FT_ERR_BAD_SIZE;
@@ -247,7 +272,7 @@ void ftx_server_s::admit(std::unique_lock<std::mutex> &lk, Req *q, Slot *sl)
 {
     q->t_admit = Clock::now();
     q->slot = (int)(sl - slots.data());
-    in_use += q->bytes;
+    in_use += q->bytes + q->out_bytes;
     running++;
     sl->req = q;
     lk.unlock();
@@ -266,7 +291,7 @@ void ftx_server_s::admit(std::unique_lock<std::mutex> &lk, Req *q, Slot *sl)
     }
     for (void *p : q->tmp) cudaFreeAsync(p, sl->st);
     q->tmp.clear();
-    in_use -= q->bytes;
+    in_use -= q->bytes + q->out_bytes;
     running--;
     sl->req = nullptr;
     q->t_done = Clock::now();
@@ -285,8 +310,13 @@ void ftx_server_s::loop()
             if (!q || !q->done) continue;
             for (void *p : q->tmp) cudaFreeAsync(p, sl.st);
             q->tmp.clear();
-            in_use -= q->bytes;
+            in_use -= q->bytes + q->out_bytes;
             running--;
+            if (q->r.op == FTX_REQ_ENCRYPT || q->r.op == FTX_REQ_SEGSUM) { // charged until released
+                resident += q->out_bytes;
+                held[q->res.c1] = q->out_bytes / 2;
+                held[q->res.c2] = q->out_bytes - q->out_bytes / 2;
+            }
             q->res.queue_ms = std::chrono::duration<double, std::milli>(q->t_admit - q->t_submit).count();
             q->res.latency_ms = std::chrono::duration<double, std::milli>(q->t_done - q->t_submit).count();
             q->finished = true;
@@ -304,7 +334,8 @@ void ftx_server_s::loop()
                 ++it;
                 continue;
             }
-            Slot *sl = in_use + q->bytes <= budget ? free_slot(q->express) : nullptr;
+            const bool fits = in_use + resident + q->bytes + q->out_bytes <= budget;
+            Slot *sl = fits ? free_slot(q->express) : nullptr;
             if (!sl) {
                 open = false;
                 ++it;
@@ -373,17 +404,22 @@ ft_error ftx_server_submit(ftx_server s, const ftx_request *req, uint64_t *ticke
         }
     }
     if (r.op != FTX_REQ_ENCRYPT && (!r.c1 || !r.c2 || r.c1->n != r.n || r.c2->n != r.n)) return FT_ERR_SIZE_MISMATCH;
+    size_t maxlen = 0;
     if (r.op == FTX_REQ_SEGSUM) {
         if (r.n >= (size_t)INT32_MAX || r.offsets[0] != 0 || (size_t)r.offsets[r.nseg] != r.n) return FT_ERR_BAD_SIZE;
-        for (size_t i = 0; i < r.nseg; ++i)
+        for (size_t i = 0; i < r.nseg; ++i) {
             if (r.offsets[i + 1] < r.offsets[i]) return FT_ERR_BAD_SIZE;
+            maxlen = std::max(maxlen, (size_t)(r.offsets[i + 1] - r.offsets[i]));
+        }
     }
     auto *q = new (std::nothrow) Req();
     if (!q) return FT_ERR_OUT_OF_MEMORY;
     q->r = r;
-    q->bytes = request_bytes(r);
+    q->seg_prefix = r.op == FTX_REQ_SEGSUM && ft::segsum_prefers_prefix(r.n, maxlen);
+    q->bytes = request_tmp_bytes(r, q->seg_prefix);
+    q->out_bytes = request_out_bytes(r);
     q->express = request_cost(r) <= EXPRESS_COST;
-    if (q->bytes > s->budget) {
+    if (q->bytes + q->out_bytes > s->budget) {
         delete q;
         return FT_ERR_INSUFFICIENT_SPACE;
     }
@@ -410,10 +446,24 @@ ft_error ftx_server_wait(ftx_server s, uint64_t ticket, ftx_result *result)
     return FT_ERR_NO_ERROR;
 }
 
+ft_error ftx_server_release(ftx_server s, ft_ge25519_array array)
+{
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->held.find(array);
+        if (it == s->held.end()) return FT_ERR_OUT_OF_BOUNDS;
+        s->resident -= it->second;
+        s->held.erase(it);
+        s->cv_work.notify_all(); // queued requests may fit now
+    }
+    ft_array_free(array); // its request has completed: nothing on the GPU uses it
+    return FT_ERR_NO_ERROR;
+}
+
 ft_error ftx_server_stats(ftx_server s, size_t *bytes_in_use, size_t *queued, size_t *running)
 {
     std::lock_guard<std::mutex> lk(s->mu);
-    *bytes_in_use = s->in_use;
+    *bytes_in_use = s->in_use + s->resident;
     *queued = s->pending.size();
     *running = s->running;
     return FT_ERR_NO_ERROR;
@@ -442,6 +492,8 @@ void ftx_server_free(ftx_server s)
     for (auto &kv : s->reqs) {
         Req *q = kv.second;
         if (q->finished && !q->res.err && (q->r.op == FTX_REQ_ENCRYPT || q->r.op == FTX_REQ_SEGSUM)) {
+            s->held.erase(q->res.c1);
+            s->held.erase(q->res.c2);
             ft_array_free(q->res.c1);
             ft_array_free(q->res.c2);
         }

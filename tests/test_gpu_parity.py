@@ -106,6 +106,43 @@ def test_contains_large_with_duplicates_and_empty(ft):
     assert (a1.contains(empty) == 0).all()
 
 
+def ref_contains(orc, a1, a2):
+    """The reference's ft_array_contains (ftcrypto.cu:1046-1070) on the
+    oracle: res[j] = OR over i of ge25519_equal(a2[i], a1[j]), where equal
+    is iszero(a2[i] - a1[j]) by the projective formulas (ftcrypto.cu:170-190)."""
+    n1, n2 = a1.shape[0], a2.shape[0]
+    eq = orc.equal(np.repeat(a2, n1, axis=0), np.tile(a1, (n2, 1))).reshape(n2, n1)
+    return eq.any(axis=0).astype(np.int64)
+
+
+def test_contains_on_and_off_the_curve(ft, orc, golden):
+    """ft_array_contains is membership of canonical encodings.  On the curve
+    that is the reference's answer.  Off the curve (the reference's results
+    for rejected encodings) it is not: the reference's projective test
+    iszero(p - q) needs the curve equation, so it reports an off-curve point
+    as absent even from an array holding the same point, while this library
+    reports it present (same encoding).  Both rules are pinned here."""
+    dec = golden["decode"]
+    pts, _ = orc.decode(hxs(c["in"] for c in dec))
+    ok = np.array([bool(c["ok"]) for c in dec])
+    g = synth.rng(17)
+    on = orc.from_scalars(synth.scalars_mod_L(g, 40), threads=4)
+    a1 = np.concatenate([pts, on])
+    a2 = np.concatenate([pts[::3], on[::2]])
+    got = ft.Array.from_packed(a1).contains(ft.Array.from_packed(a2))
+    e1, e2 = orc.encode(a1), orc.encode(a2)
+    by_encoding = (e1[:, None, :] == e2[None, :, :]).all(-1).any(axis=1).astype(np.int64)
+    assert (got == by_encoding).all()
+    ref = ref_contains(orc, a1, a2)
+    on_curve = np.concatenate([ok, np.ones(len(on), dtype=bool)])
+    assert (got[on_curve] == ref[on_curve]).all()
+    # the divergence: off-curve points found by encoding, absent for the reference
+    off = ~on_curve
+    assert off.any() and (got[off] == by_encoding[off]).all()
+    assert ((ref[off] == 0) | (got[off] == 1)).all()
+    assert (got[off] != ref[off]).any()
+
+
 def test_off_curve_points_follow_the_formulas(ft, orc, golden):
     """Decoded points include the reference's results for rejected encodings
     (not on the curve); multiplication and addition still run the same field
@@ -424,6 +461,73 @@ def test_segmented_sum_empty_and_giant_segments(ft, orc):
     with pytest.raises(ft.FtError) as e:
         ft.segmented_sum_csr(np.array([0, 5, 3, 9000], np.int32), upload(ft, a))
     assert e.value.code == 3
+
+
+def test_segmented_sum_long_segments_both_paths(ft, orc):
+    """Long segments: the host-offsets call sums the layout through one scan
+    and a difference of two prefixes per segment, the device-offsets call
+    through the walk, whose join adds the thread parts of a long segment in
+    turn; both equal the oracle, with empty segments at both ends and in the
+    middle."""
+    torch = pytest.importorskip("torch")
+    g = synth.rng(14)
+    n = 50000
+    a = rand_points(orc, g, n)
+    off = np.array([0, 0, 1, 20000, 20000, 20001, 45000, 49999, 50000, 50000], np.int32)
+    want = orc.encode(orc.segsum_csr(off, a, threads=8))
+    A = upload(ft, a)
+    assert (ft.segmented_sum_csr(off, A).to_bytes_folded() == want).all()
+    d_off = torch.from_numpy(off).cuda()
+    torch.cuda.synchronize()
+    out = ft.Array.init_scalar(len(off) - 1)
+    ft.segmented_sum_csr_device(out, d_off.data_ptr(), len(off) - 1, A)
+    assert (out.to_bytes_folded() == want).all()
+
+
+@pytest.mark.parametrize("n", [1, 2, 1000, 1 << 20])
+def test_reduce_isum_all_keys_equal(ft, orc, n):
+    """Every key the same (one segment of n points, a full reduction) and
+    two keys splitting the points unevenly, accumulated into res."""
+    g = synth.rng(500 + n)
+    src = rand_points(orc, g, min(n, 4096))
+    src = np.tile(src, (n // src.shape[0] + 1, 1))[:n].copy()
+    res = rand_points(orc, g, 5)
+    R = upload(ft, res)
+    R.reduce_isum(np.full(n, 3, np.uint64), upload(ft, src))
+    want = res.copy()
+    want[3] = orc.add(res[3:4], orc.reduce(src, threads=8))[0]
+    assert (R.to_bytes_folded() == orc.encode(want)).all()
+    keys = np.where(np.arange(n) % 97 == 5, 0, 4).astype(np.uint64)
+    R = upload(ft, res)
+    R.reduce_isum(keys, upload(ft, src))
+    w2, err = orc.isum(res, keys, src) if n <= 1000 else (None, 0)
+    if w2 is None:
+        w2 = res.copy()
+        w2[0] = orc.add(res[0:1], orc.reduce(src[keys == 0], threads=8))[0]
+        w2[4] = orc.add(res[4:5], orc.reduce(src[keys == 4], threads=8))[0]
+    assert err == 0
+    assert (R.to_bytes_folded() == orc.encode(w2)).all()
+
+
+@pytest.mark.parametrize("n", [0, 1, 5, 1000, 1025, 70001])
+@pytest.mark.parametrize("exclusive", [False, True])
+def test_ct_scan(ft, orc, n, exclusive):
+    """ftx_ct_scan: both halves in one call equal two ft_array_scan /
+    ft_array_prescan calls and the oracle; the same array passed twice is
+    scanned twice."""
+    g = synth.rng(600 + n)
+    a, b = rand_points(orc, g, n), rand_points(orc, g, n)
+    A, B = upload(ft, a), upload(ft, b)
+    ft.ct_scan(A, B, exclusive)
+    assert (A.to_bytes_folded() == orc.encode(orc.scan(a, exclusive))).all()
+    assert (B.to_bytes_folded() == orc.encode(orc.scan(b, exclusive))).all()
+    C = upload(ft, a)
+    ft.ct_scan(C, C, exclusive)
+    assert (C.to_bytes_folded() == orc.encode(orc.scan(orc.scan(a, exclusive), exclusive))).all()
+    if n:
+        with pytest.raises(ft.FtError) as e:
+            ft.ct_scan(upload(ft, a), upload(ft, b[:-1]))
+        assert e.value.code == 2
 
 
 @pytest.mark.parametrize("n,nres", [(1, 1), (50, 7), (3000, 100), (40000, 5000)])

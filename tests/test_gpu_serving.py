@@ -90,8 +90,13 @@ def test_budget_admission(ft, orc):
     ts = [srv.submit_encrypt(m, r, 1) for _ in range(4)]
     used, queued, running = srv.stats()
     assert running <= 1 and used <= per_req + 1000
-    outs = [folded(srv.wait(t)[:2]) for t in ts]
+    outs = []
+    for t in ts:  # each output handed back before the next request can fit
+        c1, c2 = srv.wait(t)[:2]
+        outs.append(folded((c1, c2)))
+        srv.release(c1, c2)
     assert all((o == outs[0]).all() for o in outs)
+    assert srv.stats()[0] == 0
     with pytest.raises(ft.FtError) as e:
         srv.submit_encrypt(np.zeros(2 * n, np.uint64), synth.scalars_mod_L(g, 2 * n), 1)
     assert e.value.code == 7  # larger than the whole budget
@@ -111,4 +116,40 @@ def test_submit_checks_and_close_with_results_pending(ft, orc):
     assert (folded(srv.wait(t)[:2]) == want).all()
     for _ in range(3):  # never collected: freed with the server
         srv.submit_encrypt(synth.plaintexts(g, 1000, 1), synth.scalars_mod_L(g, 1000), 1)
+    srv.close()
+
+
+def test_budget_counts_resident_outputs(ft, orc):
+    """Outputs the server created hold their bytes of the budget until they
+    are released: with room for two outputs, a third encrypt waits while the
+    first two are kept, and is admitted once one of them is released."""
+    import time
+    g = synth.rng(44)
+    pk = orc.encode(orc.from_scalars(synth.scalars_mod_L(g, 1)))[0]
+    n = 10000
+    out_bytes = 2 * n * 128                # the two arrays an encrypt creates
+    tmp_bytes = n * 40 + 4096              # its staged inputs while it runs
+    srv = ft.Server(pk, 2 * out_bytes + tmp_bytes + 1000, slots=4)
+    m = synth.plaintexts(g, n, 1)
+    r = synth.scalars_mod_L(g, n)
+    want = folded(ft.encrypt(pk, m, r, 1))
+    t1, t2 = srv.submit_encrypt(m, r, 1), srv.submit_encrypt(m, r, 1)
+    a1, a2 = srv.wait(t1)[:2], srv.wait(t2)[:2]
+    assert srv.stats()[0] == 2 * out_bytes
+    t3 = srv.submit_encrypt(m, r, 1)
+    deadline = time.time() + 1.0
+    while time.time() < deadline:          # the third stays queued: no room
+        used, queued, running = srv.stats()
+        assert (queued, running) == (1, 0) and used == 2 * out_bytes
+        time.sleep(0.05)
+    srv.release(*a1)                       # room for one more output
+    a3 = srv.wait(t3)[:2]
+    for a in (a2, a3):
+        assert (folded(a) == want).all()
+    srv.release(*a2)
+    srv.release(*a3)
+    assert srv.stats() == (0, 0, 0)
+    # arrays the server does not hold are refused
+    other = ft.Array.init_scalar(3)
+    assert ft.api.lib().ftx_server_release(srv._h, other.handle) == 4  # FT_ERR_OUT_OF_BOUNDS
     srv.close()
