@@ -78,6 +78,27 @@ def test_wide_products_exact(hc):
         assert v16(t) == a * a
 
 
+def test_mul_sq_words(hc):
+    """fe_mul / fe_sq return exactly fold(product): v = lo + 38 hi twice,
+    then a last + 38 for the carry (the words every coordinate depends on)."""
+    M = 2**256 - 1
+
+    def fold(t):
+        v = (t & M) + 38 * (t >> 256)
+        v = (v & M) + 38 * (v >> 256)
+        return (v & M) + 38 * (v >> 256)
+    rnd = random.Random(10)
+    vals = [0, 1, M, M - 1, 2**255 - 19, 2**255, M - 37, M - 38] + [rnd.getrandbits(256) for _ in range(3000)]
+    vals += [M - rnd.getrandbits(40) for _ in range(200)]
+    out = (ctypes.c_uint32 * 8)()
+    for i, a in enumerate(vals):
+        b = vals[(13 * i + 1) % len(vals)]
+        hc.hc_fe_mul(out, w(a), w(b))
+        assert v(out) == fold(a * b)
+        hc.hc_fe_sq(out, w(a))
+        assert v(out) == fold(a * a)
+
+
 def test_group_and_smul(hc, orc):
     g = synth.rng(3)
     n = 48
