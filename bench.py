@@ -970,8 +970,8 @@ def run_ours(args):
     return 0
 
 
-PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan", "segsum", "isum", "encode", "decode",
-                 "batch", "export")
+PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan", "ct_scan", "segsum", "isum", "encode",
+                 "decode", "batch", "export", "int_peaks")
 
 
 def run_profile(case: str, size: int | None = None) -> int:
@@ -984,6 +984,15 @@ def run_profile(case: str, size: int | None = None) -> int:
     import libftcrypto_gb300 as ft
     from libftcrypto_gb300 import synth
     ft.build()
+    if case == "int_peaks":  # the three integer probes of libftbench.so, one launch each after a warm-up
+        import ctypes
+        lib = ctypes.CDLL(os.path.join(ROOT, "libftcrypto_gb300", "libftbench.so"))
+        lib.ftb_int_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int]
+        v = (ctypes.c_double * 3)()
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        rc = lib.ftb_int_peaks(v, sms, 1)
+        print(json.dumps({"profile_case": case, "ok": rc == 0, "T_products_per_s": [x / 1e12 for x in v]}))
+        return rc
     ft.init()
     g = synth.rng(SEED + 99)
     n = size or 1 << 20
@@ -1002,7 +1011,7 @@ def run_profile(case: str, size: int | None = None) -> int:
         op = lambda: ft.encrypt_device(c1, c2, pk, m.data_ptr(), d_sc.data_ptr(), n, 8)  # noqa: E731
     elif case == "comb":
         op = lambda: ft.Array.from_scalars(sc)  # noqa: E731
-    elif case in ("add", "reduce", "scan", "segsum", "isum"):
+    elif case in ("add", "reduce", "scan", "ct_scan", "segsum", "isum"):
         big = size or (1 << 24 if case in ("reduce", "segsum") else 1 << 22)
         a = ft.Array.init_point(big, base, 3)
         a.add(ft.Array.init_point(big, base, 5))
@@ -1014,6 +1023,9 @@ def run_profile(case: str, size: int | None = None) -> int:
             op = lambda: a.reduce_into(out, 0)  # noqa: E731
         elif case == "scan":
             op = lambda: a.scan()  # noqa: E731
+        elif case == "ct_scan":  # both halves of `big` ciphertexts
+            a2 = ft.Array.init_point(big, base, 7)
+            op = lambda: ft.ct_scan(a, a2)  # noqa: E731
         elif case == "segsum":
             off = synth.csr_offsets(g, big, big // 16)
             d_off = torch.from_numpy(off).cuda()
