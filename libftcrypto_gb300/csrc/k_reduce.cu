@@ -164,7 +164,15 @@ struct ScanSet {
 #define FT_SEG_WALK_MINB 4
 #endif
 
-// per-thread sums of K consecutive points: ts[t] = sum of p[tK .. tK+K)
+#ifndef FT_WALK_PAIRS
+#define FT_WALK_PAIRS 0
+#endif
+
+// per-thread sums of K consecutive points: ts[t] = sum of p[tK .. tK+K).
+// With FT_WALK_PAIRS the thread loads its points two at a time: the two
+// 16-byte words of a pair fill one 32-byte sector of each plane, which is
+// then read from DRAM once (one point at a time, the sector's second half
+// can be evicted before the next step and read again).
 template <int K>
 __global__ void __launch_bounds__(128, FT_SCAN_SUMS_MINB) k_scan_sums(ScanSet in, size_t n, ScanSet ts)
 {
@@ -177,6 +185,27 @@ __global__ void __launch_bounds__(128, FT_SCAN_SUMS_MINB) k_scan_sums(ScanSet in
     {
         const size_t e0 = t * K;
         ge_p3 acc;
+#if FT_WALK_PAIRS
+        static_assert(K % 2 == 0, "pairs of points");
+        ge_p3 x;
+        ld_p3(acc, p, s, e0);
+        if (e0 + 1 < n) {
+            ld_p3(x, p, s, e0 + 1);
+            ge_addto(acc, x);
+        }
+#pragma unroll 1
+        for (int k = 2; k < K; k += 2) {
+            const size_t e = e0 + k;
+            if (e >= n) break;
+            ge_p3 y;
+            ld_p3(x, p, s, e);
+            const bool two = e + 1 < n;
+            if (two) ld_p3(y, p, s, e + 1);
+            ge_addto(acc, x);
+            if (!two) break;
+            ge_addto(acc, y);
+        }
+#else
         ld_p3(acc, p, s, e0);
 #pragma unroll 1
         for (int k = 1; k < K; ++k) {
@@ -186,6 +215,7 @@ __global__ void __launch_bounds__(128, FT_SCAN_SUMS_MINB) k_scan_sums(ScanSet in
             ld_p3(x, p, s, e);
             ge_addto(acc, x);
         }
+#endif
         st_p3(tp, tss, t, acc);
     }
 }
@@ -203,6 +233,25 @@ __global__ void __launch_bounds__(128, FT_SCAN_APPLY_MINB) k_scan_apply(ScanSet 
     {
         ge_p3 pre;
         ld_p3(pre, tp, tss, t);
+#if FT_WALK_PAIRS
+        static_assert(K % 2 == 0, "pairs of points");
+#pragma unroll 1
+        for (int k = 0; k < K; k += 2) {
+            const size_t e = t * K + k;
+            if (e >= n) break;
+            ge_p3 x, y;
+            ld_p3(x, p, s, e);
+            const bool two = e + 1 < n;
+            if (two) ld_p3(y, p, s, e + 1);
+            if (exclusive) st_p3(p, s, e, pre);
+            ge_addto(pre, x);
+            if (!exclusive) st_p3(p, s, e, pre);
+            if (!two) break;
+            if (exclusive) st_p3(p, s, e + 1, pre);
+            ge_addto(pre, y);
+            if (!exclusive) st_p3(p, s, e + 1, pre);
+        }
+#else
 #pragma unroll 1
         for (int k = 0; k < K; ++k) {
             const size_t e = t * K + k;
@@ -213,6 +262,7 @@ __global__ void __launch_bounds__(128, FT_SCAN_APPLY_MINB) k_scan_apply(ScanSet 
             ge_addto(pre, x);
             if (!exclusive) st_p3(p, s, e, pre);
         }
+#endif
     }
 }
 
