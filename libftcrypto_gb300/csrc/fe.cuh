@@ -48,6 +48,10 @@ FT_DEV fe fe_d() { return fe_const(0x135978a3u, 0x75eb4dcau, 0x4141d8abu, 0x0070
 FT_DEV fe fe_d2() { return fe_const(0x26b2f159u, 0xebd69b94u, 0x8283b156u, 0x00e0149au, 0xeef3d130u, 0x198e80f2u, 0x56dffce7u, 0x2406d9dcu); }
 FT_DEV fe fe_sqrtm1() { return fe_const(0x4a0ea0b0u, 0xc4ee1b27u, 0xad2fe478u, 0x2f431806u, 0x3dfbd7a7u, 0x2b4d0099u, 0x4fc1df0bu, 0x2b832480u); }
 
+#ifndef FT_ADD_ALU
+#define FT_ADD_ALU 0
+#endif
+
 // h = a + b  (h < 2^256; a carry out of bit 256 is repaid as +38)
 FT_DEV void fe_add(fe &h, const fe &a, const fe &b)
 {
@@ -56,12 +60,20 @@ FT_DEV void fe_add(fe &h, const fe &a, const fe &b)
 #pragma unroll
     for (int k = 1; k < 8; ++k) r[k] = addc_cc(a.v[k], b.v[k]);
     uint32_t c = addc(0u, 0u);
+#if FT_ADD_ALU
+    r[0] = add_cc(r[0], (0u - c) & 38u);
+#else
     r[0] = mad_lo_cc(c, 38u, r[0]);
+#endif
 #pragma unroll
     for (int k = 1; k < 8; ++k) r[k] = addc_cc(r[k], 0u);
     c = addc(0u, 0u);
     // r < 38 whenever c == 1, so this cannot carry
+#if FT_ADD_ALU
+    r[0] += (0u - c) & 38u;
+#else
     r[0] += 38u * c;
+#endif
 #pragma unroll
     for (int k = 0; k < 8; ++k) h.v[k] = r[k];
 }
@@ -94,8 +106,43 @@ FT_DEV void fe_neg(fe &h, const fe &f)
 #ifndef FT_FOLD_WIDE
 #define FT_FOLD_WIDE 1
 #endif
+#ifndef FT_FOLD_ALU
+#define FT_FOLD_ALU 0
+#endif
 
-#if FT_FOLD_WIDE
+#if FT_FOLD_ALU
+// 512-bit t -> h < 2^256 with 2^256 = 38 (mod p), with 38 t_hi formed as
+// (t_hi << 5) + (t_hi << 2) + (t_hi << 1) by funnel shifts and carry chains
+// on the ALU pipe, which the multiplications leave half idle, instead of
+// eight more 32x32->64 products on the multiply-add pipe that binds them.
+// A = t_lo + (t_hi << 5) and B = (t_hi << 2) + (t_hi << 1) are independent
+// chains; r = A + B < 39 * 2^256, whose top word is folded once more.
+FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
+{
+    const uint32_t *H = t + 8;
+    uint32_t A[9], B[9], r[8];
+    A[0] = add_cc(t[0], H[0] << 5);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) A[k] = addc_cc(t[k], shl_w(H[k - 1], H[k], 5));
+    A[8] = addc(H[7] >> 27, 0u);
+    B[0] = add_cc(H[0] << 2, H[0] << 1);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) B[k] = addc_cc(shl_w(H[k - 1], H[k], 2), shl_w(H[k - 1], H[k], 1));
+    B[8] = addc(H[7] >> 30, H[7] >> 31);
+    r[0] = add_cc(A[0], B[0]);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r[k] = addc_cc(A[k], B[k]);
+    const uint32_t r8 = addc(A[8], B[8]);
+    // value = r + r8 * 2^256 with r8 <= 38
+    r[0] = mad_lo_cc(r8, 38u, r[0]);
+#pragma unroll
+    for (int k = 1; k < 8; ++k) r[k] = addc_cc(r[k], 0u);
+    uint32_t c = addc(0u, 0u);
+    r[0] += 38u * c; // r < 1482 whenever c == 1
+#pragma unroll
+    for (int k = 0; k < 8; ++k) h.v[k] = r[k];
+}
+#elif FT_FOLD_WIDE
 // 512-bit t -> h < 2^256 with 2^256 = 38 (mod p).  r = t_lo + 38 t_hi as
 // 64-bit windows of 38 * t[8 + k] at position k, in even-aligned register
 // pairs as in mul_wide: the even k in one carry chain over t_lo, the odd k
@@ -160,100 +207,7 @@ FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
 #define FT_MUL_ALIGNED 1
 #endif
 
-#ifndef FT_MUL_KARATSUBA
-#define FT_MUL_KARATSUBA 0
-#endif
-
-// r = x * y for 4-limb x, y (256-bit product), in the aligned windows of
-// mul_wide below: even positions in E, odd ones in O one word lower
-FT_DEV void mul4_wide(uint32_t r[8], const uint32_t x[4], const uint32_t y[4])
-{
-    uint32_t E[8], O[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) E[k] = O[k] = 0u;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int je = i & 1, jo = je ^ 1;
-        E[i + je] = mad_lo_cc(x[je], y[i], E[i + je]);
-        E[i + je + 1] = madc_hi_cc(x[je], y[i], E[i + je + 1]);
-        E[i + je + 2] = madc_lo_cc(x[je + 2], y[i], E[i + je + 2]);
-        E[i + je + 3] = madc_hi_cc(x[je + 2], y[i], E[i + je + 3]);
-        if (i + je + 4 < 8) E[i + je + 4] = addc(E[i + je + 4], 0u);
-        O[i + jo - 1] = mad_lo_cc(x[jo], y[i], O[i + jo - 1]);
-        O[i + jo] = madc_hi_cc(x[jo], y[i], O[i + jo]);
-        O[i + jo + 1] = madc_lo_cc(x[jo + 2], y[i], O[i + jo + 1]);
-        O[i + jo + 2] = madc_hi_cc(x[jo + 2], y[i], O[i + jo + 2]);
-        if (i + jo + 3 < 8) O[i + jo + 3] = addc(O[i + jo + 3], 0u);
-    }
-    r[0] = E[0];
-    r[1] = add_cc(E[1], O[0]);
-#pragma unroll
-    for (int k = 2; k < 7; ++k) r[k] = addc_cc(E[k], O[k - 1]);
-    r[7] = addc(E[7], O[6]);
-}
-
-#if FT_MUL_KARATSUBA
-// t = a * b (full 512-bit product) by one level of Karatsuba over 128-bit
-// halves: z0 = aL bL, z2 = aH bH, z1 = (aL + aH)(bL + bH) - z0 - z2, with
-// the 129-bit sums' top bits added in as masked 128-bit shifts.  Three
-// 4 x 4 limb products (48 multiplications instead of 64) for about 55 more
-// additions on the ALU pipe; the product is exact, so the words are those
-// of the schoolbook.
-FT_DEV void mul_wide(uint32_t t[16], const fe &a, const fe &b)
-{
-    uint32_t aL[4], aH[4], bL[4], bH[4], sa[4], sb[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        aL[k] = a.v[k];
-        aH[k] = a.v[k + 4];
-        bL[k] = b.v[k];
-        bH[k] = b.v[k + 4];
-    }
-    sa[0] = add_cc(aL[0], aH[0]);
-#pragma unroll
-    for (int k = 1; k < 4; ++k) sa[k] = addc_cc(aL[k], aH[k]);
-    const uint32_t ca = addc(0u, 0u);
-    sb[0] = add_cc(bL[0], bH[0]);
-#pragma unroll
-    for (int k = 1; k < 4; ++k) sb[k] = addc_cc(bL[k], bH[k]);
-    const uint32_t cb = addc(0u, 0u);
-    uint32_t z0[8], z2[8], m[8];
-    mul4_wide(z0, aL, bL);
-    mul4_wide(z2, aH, bH);
-    mul4_wide(m, sa, sb);
-    // (sa + ca 2^128)(sb + cb 2^128) = m + (ca sb + cb sa) 2^128 + ca cb 2^256
-    const uint32_t mka = 0u - ca, mkb = 0u - cb;
-    m[4] = add_cc(m[4], sb[0] & mka);
-#pragma unroll
-    for (int k = 5; k < 8; ++k) m[k] = addc_cc(m[k], sb[k - 4] & mka);
-    uint32_t m8 = addc(ca & cb, 0u);
-    m[4] = add_cc(m[4], sa[0] & mkb);
-#pragma unroll
-    for (int k = 5; k < 8; ++k) m[k] = addc_cc(m[k], sa[k - 4] & mkb);
-    m8 = addc(m8, 0u);
-    // z1 = that - z0 - z2 = aL bH + aH bL < 2^257
-    m[0] = sub_cc(m[0], z0[0]);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) m[k] = subc_cc(m[k], z0[k]);
-    m8 = subc(m8, 0u);
-    m[0] = sub_cc(m[0], z2[0]);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) m[k] = subc_cc(m[k], z2[k]);
-    m8 = subc(m8, 0u);
-    // t = z0 + z1 2^128 + z2 2^256
-#pragma unroll
-    for (int k = 0; k < 4; ++k) t[k] = z0[k];
-    t[4] = add_cc(z0[4], m[0]);
-#pragma unroll
-    for (int k = 5; k < 8; ++k) t[k] = addc_cc(z0[k], m[k - 4]);
-#pragma unroll
-    for (int k = 8; k < 12; ++k) t[k] = addc_cc(z2[k - 8], m[k - 4]);
-    t[12] = addc_cc(z2[4], m8);
-    t[13] = addc_cc(z2[5], 0u);
-    t[14] = addc_cc(z2[6], 0u);
-    t[15] = addc(z2[7], 0u);
-}
-#elif FT_MUL_ALIGNED
+#if FT_MUL_ALIGNED
 // t = a * b (full 512-bit product).  Each product a_j * b_i is one 64-bit
 // window (lo at position p = i + j, hi at p + 1) that ptxas computes with
 // one IMAD.WIDE into an even-aligned register pair.  Windows at even p

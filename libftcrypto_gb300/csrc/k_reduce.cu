@@ -165,14 +165,17 @@ struct ScanSet {
 #endif
 
 #ifndef FT_WALK_PAIRS
-#define FT_WALK_PAIRS 0
+#define FT_WALK_PAIRS 1
 #endif
 
 // per-thread sums of K consecutive points: ts[t] = sum of p[tK .. tK+K).
 // With FT_WALK_PAIRS the thread loads its points two at a time: the two
 // 16-byte words of a pair fill one 32-byte sector of each plane, which is
 // then read from DRAM once (one point at a time, the sector's second half
-// can be evicted before the next step and read again).
+// can be evicted before the next step and read again: 1.29x the
+// algorithmic bytes in the sums, 1.39x in the rescan, measured), and the
+// rescan waits for memory once per two points.  2 x 4,194,304-point
+// ciphertext scan: 2.045 -> 2.020 ms.
 template <int K>
 __global__ void __launch_bounds__(128, FT_SCAN_SUMS_MINB) k_scan_sums(ScanSet in, size_t n, ScanSet ts)
 {
