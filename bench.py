@@ -179,7 +179,7 @@ def profile_traffic():
 
 def imad_peak(sm_count: int):
     """32x32->64 products per second of the mad.wide.u32 probe alone
-    (libftbench.so; its ncu summary is profiles/k_imad_wide_peak.md)."""
+    (libftbench.so; its ncu summary is profiles/k_imad_int_peaks.md)."""
     import ctypes
     lib = ctypes.CDLL(os.path.join(ROOT, "libftcrypto_gb300", "libftbench.so"))
     lib.ftb_imad_wide_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]

@@ -106,50 +106,16 @@ FT_DEV void fe_neg(fe &h, const fe &f)
 #ifndef FT_FOLD_WIDE
 #define FT_FOLD_WIDE 1
 #endif
-#ifndef FT_FOLD_ALU
-#define FT_FOLD_ALU 0
-#endif
-
-#if FT_FOLD_ALU
-// 512-bit t -> h < 2^256 with 2^256 = 38 (mod p), with 38 t_hi formed as
-// (t_hi << 5) + (t_hi << 2) + (t_hi << 1) by funnel shifts and carry chains
-// on the ALU pipe, which the multiplications leave half idle, instead of
-// eight more 32x32->64 products on the multiply-add pipe that binds them.
-// A = t_lo + (t_hi << 5) and B = (t_hi << 2) + (t_hi << 1) are independent
-// chains; r = A + B < 39 * 2^256, whose top word is folded once more.
-FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
-{
-    const uint32_t *H = t + 8;
-    uint32_t A[9], B[9], r[8];
-    A[0] = add_cc(t[0], H[0] << 5);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) A[k] = addc_cc(t[k], shl_w(H[k - 1], H[k], 5));
-    A[8] = addc(H[7] >> 27, 0u);
-    B[0] = add_cc(H[0] << 2, H[0] << 1);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) B[k] = addc_cc(shl_w(H[k - 1], H[k], 2), shl_w(H[k - 1], H[k], 1));
-    B[8] = addc(H[7] >> 30, H[7] >> 31);
-    r[0] = add_cc(A[0], B[0]);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) r[k] = addc_cc(A[k], B[k]);
-    const uint32_t r8 = addc(A[8], B[8]);
-    // value = r + r8 * 2^256 with r8 <= 38
-    r[0] = mad_lo_cc(r8, 38u, r[0]);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) r[k] = addc_cc(r[k], 0u);
-    uint32_t c = addc(0u, 0u);
-    r[0] += 38u * c; // r < 1482 whenever c == 1
-#pragma unroll
-    for (int k = 0; k < 8; ++k) h.v[k] = r[k];
-}
-#elif FT_FOLD_WIDE
+#if FT_FOLD_WIDE
 // 512-bit t -> h < 2^256 with 2^256 = 38 (mod p).  r = t_lo + 38 t_hi as
 // 64-bit windows of 38 * t[8 + k] at position k, in even-aligned register
 // pairs as in mul_wide: the even k in one carry chain over t_lo, the odd k
 // in a second array one word lower (the windows there do not overlap: no
 // carries), then added; the top word (at most 38) is folded once more.
 // Measured against the row-by-row fold below: 21.4 -> 20.4 ms for the
-// constant-time ladder of 1,048,576 points, same words.
+// constant-time ladder of 1,048,576 points, same words.  (Forming 38 t_hi
+// as (t_hi << 5) + (t_hi << 2) + (t_hi << 1) with funnel shifts and carry
+// chains instead measured slower: 23.7 ms.)
 FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
 {
     uint32_t r[8], r8, o[8];

@@ -23,5 +23,3 @@ FT_DEV uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm
 FT_DEV uint32_t madc_hi(uint32_t a, uint32_t b, uint32_t c) { uint32_t r; asm volatile("madc.hi.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c)); return r; }
 FT_DEV uint32_t mul_lo(uint32_t a, uint32_t b) { return a * b; }
 FT_DEV uint32_t mul_hi(uint32_t a, uint32_t b) { return __umulhi(a, b); }
-// bits [32 - s, 64 - s) of the 64-bit hi:lo, i.e. the word (hi << s) | (lo >> (32 - s)), 0 < s < 32
-FT_DEV uint32_t shl_w(uint32_t lo, uint32_t hi, uint32_t s) { return __funnelshift_l(lo, hi, s); }

@@ -26,7 +26,6 @@ static inline uint32_t madc_hi_cc(uint32_t a, uint32_t b, uint32_t c) { uint64_t
 static inline uint32_t madc_hi(uint32_t a, uint32_t b, uint32_t c) { return (uint32_t)(((uint64_t)a * b) >> 32) + c + g_cf; }
 static inline uint32_t mul_lo(uint32_t a, uint32_t b) { return a * b; }
 static inline uint32_t mul_hi(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
-static inline uint32_t shl_w(uint32_t lo, uint32_t hi, uint32_t s) { return (uint32_t)(((((uint64_t)hi << 32) | lo) << s) >> 32); }
 
 // 16-byte word of the device code (CUDA's uint4)
 struct uint4 {
