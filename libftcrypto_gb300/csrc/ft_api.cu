@@ -12,6 +12,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <new>
 #include <set>
 #include <vector>
 
@@ -47,6 +48,20 @@ struct Ctx {
     uint32_t *b_table = nullptr;  // radix-32 comb table of B (fixed-base products)
     void *dlog_mem = nullptr;     // decryption table of j*B, j < dlog.m_max
     ft::DlogTable dlog;
+    // Transfers that overlap queued kernels (see export_begin, stage_scalars):
+    // a second stream at the device's highest priority, an export buffer used
+    // only on it, and two staging buffers for host scalars, each with the
+    // events of its copy and of the kernel that read it.
+    cudaStream_t xfer = nullptr;
+    void *xscratch = nullptr;
+    size_t xscratch_cap = 0;
+    struct Stage {
+        void *p = nullptr;
+        size_t cap = 0;
+        cudaEvent_t copied = nullptr, consumed = nullptr;
+    };
+    Stage stage[2];
+    int stage_next = 0;
 };
 
 Ctx g;
@@ -132,13 +147,107 @@ cudaError_t h2d(void *dst, const void *src, size_t bytes)
     return e;
 }
 
-cudaError_t d2h(void *dst, const void *src, size_t bytes)
+cudaError_t d2h(void *dst, const void *src, size_t bytes, cudaStream_t st = nullptr)
 {
+    if (!st) st = g.stream;
     if (bytes) {
-        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g.stream);
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) return e;
     }
-    return cudaStreamSynchronize(g.stream);
+    return cudaStreamSynchronize(st);
+}
+
+// Marks that the work just queued on the library stream completes a's
+// writes: an export of a that follows, with no other use of a in between,
+// waits for this point only (export_begin), not for everything queued after.
+cudaError_t mark_ready(const_ft_ge25519_array ca)
+{
+    auto *a = const_cast<ft_ge25519_array_s *>(ca);
+    if (a->exposed.load()) return cudaSuccess;
+    if (!a->ready) {
+        cudaError_t e = cudaEventCreateWithFlags(&a->ready, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            a->ready = nullptr;
+            return e;
+        }
+    }
+    a->ready_touch = a->touch.load();
+    return cudaEventRecord(a->ready, g.stream);
+}
+
+// The stream and the device buffer (at least `bytes`) an export of a
+// converts and copies on.  When the call that last wrote a marked it and
+// nothing has used a since, that is the transfer stream after a wait for
+// the mark: the conversion and the device-to-host copy then overlap kernels
+// queued later on the library stream (an export of c1 runs during the
+// scalar multiplication of c2).  Otherwise the library stream and its
+// scratch, in order.  The export buffer is only ever used on the transfer
+// stream, and every export ends with that stream synchronised.
+cudaError_t export_begin(const_ft_ge25519_array a, size_t bytes, void **buf, cudaStream_t *st)
+{
+    const bool side = a->ready && !a->exposed.load() && a->touch.load() == a->ready_touch;
+    if (!side) {
+        *st = g.stream;
+        return scratch(buf, bytes);
+    }
+    cudaError_t e;
+    if (bytes > g.xscratch_cap) {
+        if (g.xscratch) cudaFreeAsync(g.xscratch, g.xfer);
+        g.xscratch = nullptr;
+        g.xscratch_cap = 0;
+        size_t cap = std::max(bytes, (size_t)1 << 20);
+        if ((e = cudaMallocFromPoolAsync(&g.xscratch, cap, g.pool, g.xfer)) != cudaSuccess) return e;
+        g.xscratch_cap = cap;
+    }
+    if ((e = cudaStreamWaitEvent(g.xfer, a->ready, 0)) != cudaSuccess) return e;
+    *buf = g.xscratch;
+    *st = g.xfer;
+    return cudaSuccess;
+}
+
+// the storage of a as a view, without counting a use (an export reads it on
+// the stream export_begin chose)
+View export_view(const_ft_ge25519_array a) { return View{a->planes, a->cap}; }
+
+// Copies `bytes` of pinned host memory into one of two staging buffers on
+// the transfer stream, so that the copy overlaps kernels already queued on
+// the library stream.  A buffer is refilled only after the kernel that last
+// read it has finished (its `consumed` event, which the caller records after
+// the kernel that reads this copy), and the library stream waits for the
+// copy (`copied`) before that kernel.  The caller waits for `copied` before
+// returning, so its buffer may be reused at once.
+cudaError_t stage_scalars(void **out, Ctx::Stage **sgp, const void *src, size_t bytes)
+{
+    Ctx::Stage &sg = g.stage[g.stage_next];
+    g.stage_next ^= 1;
+    cudaError_t e;
+    if (!sg.copied) {
+        cudaEvent_t c1 = nullptr, c2 = nullptr;
+        if ((e = cudaEventCreateWithFlags(&c1, cudaEventDisableTiming)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&c2, cudaEventDisableTiming)) != cudaSuccess) {
+            cudaEventDestroy(c1);
+            return e;
+        }
+        sg.copied = c1;
+        sg.consumed = c2; // never recorded yet: a wait on it returns at once
+    }
+    if (bytes > sg.cap) {
+        // a kernel queued earlier may still read the old buffer: it is freed
+        // in the library stream's order, after that kernel
+        if (sg.p) cudaFreeAsync(sg.p, g.stream);
+        sg.p = nullptr;
+        sg.cap = 0;
+        size_t cap = std::max(bytes, (size_t)1 << 20);
+        if ((e = cudaMallocFromPoolAsync(&sg.p, cap, g.pool, g.xfer)) != cudaSuccess) return e;
+        sg.cap = cap;
+    }
+    if ((e = cudaStreamWaitEvent(g.xfer, sg.consumed, 0)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(sg.p, src, bytes, cudaMemcpyHostToDevice, g.xfer)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(sg.copied, g.xfer)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(g.stream, sg.copied, 0)) != cudaSuccess) return e;
+    *out = sg.p;
+    *sgp = &sg;
+    return cudaSuccess;
 }
 
 // arrays whose byte sizes (160 per point at most, in exports) overflow size_t
@@ -148,14 +257,13 @@ bool too_long(size_t n) { return n > SIZE_MAX / 256; }
 ft_error arr_new(ft_ge25519_array *out, size_t n)
 {
     if (too_long(n)) return FT_ERR_OUT_OF_MEMORY;
-    auto *a = (ft_ge25519_array_s *)std::malloc(sizeof(ft_ge25519_array_s));
+    auto *a = new (std::nothrow) ft_ge25519_array_s();
     if (!a) return FT_ERR_OUT_OF_MEMORY;
     a->n = n;
     a->cap = n;
-    a->planes = nullptr;
     cudaError_t e = dev_alloc((void **)&a->planes, n * FT_PLANES_BYTES_PER_POINT);
     if (e != cudaSuccess) {
-        std::free(a);
+        delete a;
         return map_err(e);
     }
     *out = a;
@@ -352,6 +460,9 @@ namespace {
 ft_error init_device(int dev)
 {
     CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+    int prio_lo = 0, prio_hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    CK(cudaStreamCreateWithPriority(&g.xfer, cudaStreamNonBlocking, prio_hi));
     cudaMemPoolProps pp;
     std::memset(&pp, 0, sizeof pp);
     pp.allocType = cudaMemAllocationTypePinned;
@@ -385,7 +496,13 @@ ft_error init_device(int dev)
 void init_release()
 {
     if (g.stream) cudaStreamSynchronize(g.stream);
+    if (g.xfer) cudaStreamSynchronize(g.xfer);
+    for (auto &sg : g.stage) {
+        if (sg.copied) cudaEventDestroy(sg.copied);
+        if (sg.consumed) cudaEventDestroy(sg.consumed);
+    }
     if (g.pool) cudaMemPoolDestroy(g.pool); // releases its memory once nothing is outstanding
+    if (g.xfer) cudaStreamDestroy(g.xfer);
     if (g.stream) cudaStreamDestroy(g.stream);
     cudaGetLastError();
     g = Ctx{};
@@ -567,9 +684,10 @@ ft_error ft_array_to_bytes_folded(uint8_t *mem, size_t n_bytes, const_ft_ge25519
     if (n_bytes / FT_FOLDED_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
     if (n == 0) return FT_ERR_NO_ERROR;
     void *s;
-    CK(scratch(&s, align256(n * 32)));
-    CK(ft::encode((uint8_t *)s, ft::view_of(array), n, g.stream));
-    CK(d2h(mem, s, n * 32));
+    cudaStream_t st;
+    CK(export_begin(array, align256(n * 32), &s, &st));
+    CK(ft::encode((uint8_t *)s, export_view(array), n, st));
+    CK(d2h(mem, s, n * 32, st));
     return FT_ERR_NO_ERROR;
 }
 
@@ -580,9 +698,10 @@ ft_error ft_array_to_bytes_affine(uint8_t *mem, size_t n_bytes, const_ft_ge25519
     if (n_bytes / FT_AFFINE_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
     if (n == 0) return FT_ERR_NO_ERROR;
     void *s;
-    CK(scratch(&s, align256(n * 64)));
-    CK(ft::to_affine((uint8_t *)s, ft::view_of(array), n, g.stream));
-    CK(d2h(mem, s, n * 64));
+    cudaStream_t st;
+    CK(export_begin(array, align256(n * 64), &s, &st));
+    CK(ft::to_affine((uint8_t *)s, export_view(array), n, st));
+    CK(d2h(mem, s, n * 64, st));
     return FT_ERR_NO_ERROR;
 }
 
@@ -593,9 +712,10 @@ ft_error ft_array_to_bytes(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array 
     if (n_bytes / FT_EXTENDED_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
     if (n == 0) return FT_ERR_NO_ERROR;
     void *s;
-    CK(scratch(&s, align256(n * 160)));
-    CK(ft::to_ref160((uint8_t *)s, ft::view_of(array), n, g.stream));
-    CK(d2h(mem, s, n * 160));
+    cudaStream_t st;
+    CK(export_begin(array, align256(n * 160), &s, &st));
+    CK(ft::to_ref160((uint8_t *)s, export_view(array), n, st));
+    CK(d2h(mem, s, n * 160, st));
     return FT_ERR_NO_ERROR;
 }
 
@@ -689,7 +809,8 @@ void ft_array_free(ft_ge25519_array array)
 {
     if (!array) return;
     if (g.inited) dev_free(array->planes);
-    std::free(array);
+    if (array->ready) cudaEventDestroy(array->ready);
+    delete array;
 }
 
 size_t ft_array_get_length(const_ft_ge25519_array array) { return array->n; }
@@ -848,10 +969,22 @@ ft_error ft_mul(ft_ge25519_array array, const uint8_t *scalars, size_t n)
     ENSURE_INIT();
     if (n != array->n) return FT_ERR_SIZE_MISMATCH;
     if (n == 0) return FT_ERR_NO_ERROR;
-    void *s;
-    CK(scratch(&s, align256(n * 32)));
-    CK(h2d(s, scalars, n * 32));
+    const void *s;
+    Ctx::Stage *sg = nullptr;
+    if (host_is_pinned(scalars)) {
+        void *p;
+        CK(stage_scalars(&p, &sg, scalars, n * 32));
+        s = p;
+    } else {
+        void *p;
+        CK(scratch(&p, align256(n * 32)));
+        CK(h2d(p, scalars, n * 32));
+        s = p;
+    }
     CK(ft::smul_var(ft::view_of(array), n, (const uint8_t *)s, 1, g.stream));
+    if (sg) CK(cudaEventRecord(sg->consumed, g.stream));
+    CK(mark_ready(array));
+    if (sg) CK(cudaEventSynchronize(sg->copied)); // the caller may reuse its buffer
     return FT_ERR_NO_ERROR;
 }
 
@@ -958,6 +1091,7 @@ ft_error ftx_synchronize(void)
 
 ft_error ftx_array_device_view(const_ft_ge25519_array array, void **planes, size_t *stride)
 {
+    array->exposed.store(true); // the caller may write it where the library cannot see
     *planes = (void *)array->planes;
     *stride = array->cap;
     return FT_ERR_NO_ERROR;
@@ -970,9 +1104,10 @@ ft_error ftx_array_to_packed(uint8_t *mem, size_t n_bytes, const_ft_ge25519_arra
     if (n_bytes / 128 < n) return FT_ERR_INSUFFICIENT_SPACE;
     if (n == 0) return FT_ERR_NO_ERROR;
     void *s;
-    CK(scratch(&s, align256(n * 128)));
-    CK(ft::to_packed((uint8_t *)s, ft::view_of(array), n, g.stream));
-    CK(d2h(mem, s, n * 128));
+    cudaStream_t st;
+    CK(export_begin(array, align256(n * 128), &s, &st));
+    CK(ft::to_packed((uint8_t *)s, export_view(array), n, st));
+    CK(d2h(mem, s, n * 128, st));
     return FT_ERR_NO_ERROR;
 }
 
@@ -996,6 +1131,7 @@ ft_error ftx_mul_device(ft_ge25519_array array, const uint8_t *d_scalars, size_t
     ENSURE_INIT();
     if (n != array->n) return FT_ERR_SIZE_MISMATCH;
     CK(ft::smul_var(ft::view_of(array), n, d_scalars, 1, g.stream));
+    CK(mark_ready(array));
     return FT_ERR_NO_ERROR;
 }
 
@@ -1011,6 +1147,8 @@ ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint
     ft_error err = ensure_pk_table(pk, &tab);
     if (err) return err;
     CK(ft::encrypt(ft::view_of(c1), ft::view_of(c2), n, d_r, d_m, m_digits(bits), tab, g.stream));
+    CK(mark_ready(c1));
+    CK(mark_ready(c2));
     return FT_ERR_NO_ERROR;
 }
 
@@ -1044,6 +1182,8 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
     }
     cudaError_t e = ft::encrypt(ft::view_of(a), ft::view_of(b), n, (const uint8_t *)s,
                                 (const uint64_t *)((uint8_t *)s + br), m_digits(bits), tab, g.stream);
+    if (e == cudaSuccess) e = mark_ready(a);
+    if (e == cudaSuccess) e = mark_ready(b);
     if (e != cudaSuccess) {
         ft_array_free(a);
         ft_array_free(b);
@@ -1443,6 +1583,7 @@ ft_error ftx_batch_run(ftx_batch b)
     ENSURE_INIT();
     for (const auto &r : b->arrays)
         if (r.a->planes != r.planes || r.a->cap != r.cap || r.a->n != r.n) return FT_ERR_SIZE_MISMATCH;
+    for (const auto &r : b->arrays) r.a->touch.fetch_add(1); // the run hands their storage to the kernel
     if (!b->ready) {
         ft_error err = batch_upload(b);
         if (err) return err;

@@ -14,10 +14,23 @@
 #define FT_PLANES_BYTES_PER_POINT ((size_t)FT_PLANES * 16)
 
 // An array handle: device-resident structure-of-arrays planes (points.cuh).
+// Allocated with new / freed with delete (ft_api.cu, serve.cu).
 struct ft_ge25519_array_s {
-    uint4 *planes; // FT_PLANES planes of `cap` uint4 each (NULL when cap == 0)
-    size_t n;      // number of points
-    size_t cap;    // plane stride = number of points allocated
+    uint4 *planes = nullptr; // FT_PLANES planes of `cap` uint4 each (NULL when cap == 0)
+    size_t n = 0;            // number of points
+    size_t cap = 0;          // plane stride = number of points allocated
+    // Host-side bookkeeping for exports that overlap queued work (ft_api.cu):
+    // `touch` counts every hand-over of the storage to device work
+    // (ft::view_of, reallocation, a batch run); `ready` is an event recorded
+    // on the library stream right after a call that wrote the array marked
+    // it (mark_ready), and stays valid while `touch` equals `ready_touch`.
+    // `exposed`: the device address was handed out (ftx_array_device_view),
+    // so writes the library does not see may follow and exports stay in
+    // stream order.
+    mutable std::atomic<uint64_t> touch{0};
+    cudaEvent_t ready = nullptr;
+    uint64_t ready_touch = 0;
+    mutable std::atomic<bool> exposed{false};
 };
 
 namespace ft {
@@ -42,7 +55,11 @@ struct View {
     size_t s; // plane stride
 };
 
-inline View view_of(const ft_ge25519_array_s *a, size_t off = 0) { return View{a->planes + off, a->cap}; }
+inline View view_of(const ft_ge25519_array_s *a, size_t off = 0)
+{
+    a->touch.fetch_add(1, std::memory_order_relaxed);
+    return View{a->planes + off, a->cap};
+}
 
 // ---- element-wise (k_elem.cu)
 cudaError_t set_zero(View v, size_t n, cudaStream_t st);

@@ -26,6 +26,7 @@
 // the budget bounds what the server keeps resident, not only what is in
 // flight.
 #include <algorithm>
+#include <new>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -156,14 +157,13 @@ static cudaError_t alloc_on(Req *q, void **p, size_t bytes, cudaStream_t st)
 
 static cudaError_t new_array(ft_ge25519_array *out, size_t n, cudaStream_t st)
 {
-    auto *a = (ft_ge25519_array_s *)std::malloc(sizeof(ft_ge25519_array_s));
+    auto *a = new (std::nothrow) ft_ge25519_array_s();
     if (!a) return cudaErrorMemoryAllocation;
     a->n = a->cap = n;
-    a->planes = nullptr;
     cudaError_t e = n ? cudaMallocFromPoolAsync((void **)&a->planes, n * FT_PLANES_BYTES_PER_POINT, ft::host_pool(), st)
                       : cudaSuccess;
     if (e != cudaSuccess) {
-        std::free(a);
+        delete a;
         return e;
     }
     *out = a;
@@ -285,7 +285,7 @@ void ftx_server_s::admit(std::unique_lock<std::mutex> &lk, Req *q, Slot *sl)
         for (ft_ge25519_array *a : {&q->res.c1, &q->res.c2})
             if (*a) {
                 if ((*a)->planes) cudaFreeAsync((*a)->planes, sl->st);
-                std::free(*a);
+                delete *a;
                 *a = nullptr;
             }
     }
