@@ -163,9 +163,7 @@ struct ScanSet {
 #ifndef FT_SEG_WALK_MINB
 #define FT_SEG_WALK_MINB 4
 #endif
-#ifndef FT_SEG_PAIRS
-#define FT_SEG_PAIRS 0
-#endif
+
 
 #ifndef FT_WALK_PAIRS
 #define FT_WALK_PAIRS 1
@@ -444,9 +442,6 @@ __global__ void __launch_bounds__(128, FT_SEG_WALK_MINB) k_seg_walk(uint4 *op, s
         // the warps stay on the same stretch of code and share the
         // instruction caches (instruction-fetch stalls were 1.45 per issue):
         // 2.32 -> 2.21 ms for 16,777,216 points in 1,048,576 segments
-#if FT_SEG_PAIRS
-        ge_p3 y;
-#endif
 #pragma unroll 1
         for (int k = 0; k < K; ++k) {
             __syncthreads();
@@ -454,16 +449,7 @@ __global__ void __launch_bounds__(128, FT_SEG_WALK_MINB) k_seg_walk(uint4 *op, s
             if (e >= e1) continue;
             while ((long long)off[sg + 1] <= e) ++sg;
             ge_p3 x;
-#if FT_SEG_PAIRS
-            if ((k & 1) == 0) {
-                ld_p3(x, sp, ss, perm ? (size_t)perm[e] : (size_t)e);
-                if (e + 1 < e1) ld_p3(y, sp, ss, perm ? (size_t)perm[e + 1] : (size_t)e + 1);
-            } else {
-                x = y;
-            }
-#else
             ld_p3(x, sp, ss, perm ? (size_t)perm[e] : (size_t)e);
-#endif
             if ((long long)off[sg] == e || e == e0) acc = x;
             else ge_addto(acc, x);
             if ((long long)off[sg + 1] == e + 1) { // last point of segment sg
