@@ -91,19 +91,15 @@ FT_DEV void fe_neg(fe &h, const fe &f)
     fe_sub(h, z, f);
 }
 
-#ifndef FT_FOLD_WIDE
-#define FT_FOLD_WIDE 1
-#endif
-#if FT_FOLD_WIDE
 // 512-bit t -> h < 2^256 with 2^256 = 38 (mod p).  r = t_lo + 38 t_hi as
 // 64-bit windows of 38 * t[8 + k] at position k, in even-aligned register
 // pairs as in mul_wide: the even k in one carry chain over t_lo, the odd k
 // in a second array one word lower (the windows there do not overlap: no
 // carries), then added; the top word (at most 38) is folded once more.
-// Measured against the row-by-row fold below: 21.4 -> 20.4 ms for the
-// constant-time ladder of 1,048,576 points, same words.  (Forming 38 t_hi
-// as (t_hi << 5) + (t_hi << 2) + (t_hi << 1) with funnel shifts and carry
-// chains instead measured slower: 23.7 ms.)
+// Measured against a fold of row-by-row (lo, then hi) chains: 21.4 -> 20.4
+// ms for the constant-time ladder of 1,048,576 points, same words.
+// (Forming 38 t_hi as (t_hi << 5) + (t_hi << 2) + (t_hi << 1) with funnel
+// shifts and carry chains instead measured slower: 23.7 ms.)
 FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
 {
     uint32_t r[8], r8, o[8];
@@ -133,34 +129,7 @@ FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
 #pragma unroll
     for (int k = 0; k < 8; ++k) h.v[k] = r[k];
 }
-#else
-// 512-bit t -> h < 2^256 with 2^256 = 38 (mod p)
-FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
-{
-    uint32_t r[8], r8;
-    r[0] = mad_lo_cc(t[8], 38u, t[0]);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) r[k] = madc_lo_cc(t[8 + k], 38u, t[k]);
-    r8 = addc(0u, 0u);
-    r[1] = mad_hi_cc(t[8], 38u, r[1]);
-#pragma unroll
-    for (int k = 2; k < 8; ++k) r[k] = madc_hi_cc(t[7 + k], 38u, r[k]);
-    r8 = madc_hi(t[15], 38u, r8);
-    // value = r + r8 * 2^256 with r8 <= 38
-    r[0] = mad_lo_cc(r8, 38u, r[0]);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) r[k] = addc_cc(r[k], 0u);
-    uint32_t c = addc(0u, 0u);
-    r[0] += 38u * c; // r < 1482 whenever c == 1
-#pragma unroll
-    for (int k = 0; k < 8; ++k) h.v[k] = r[k];
-}
-#endif
 
-#ifndef FT_MUL_ALIGNED
-#define FT_MUL_ALIGNED 1
-#endif
-#if FT_MUL_ALIGNED
 // t = a * b (full 512-bit product).  Each product a_j * b_i is one 64-bit
 // window (lo at position p = i + j, hi at p + 1) that ptxas computes with
 // one IMAD.WIDE into an even-aligned register pair.  Windows at even p
@@ -174,132 +143,105 @@ FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
 // Field-multiplication throughput of other schedules, measured: one level of
 // Karatsuba (48 products and ~55 more additions) 7.08 T products/s, four
 // independent 4 x 4 blocks 6.83, this one 7.89.
-FT_DEV void mul_wide(uint32_t t[16], const fe &a, const fe &b)
+FT_DEV void mul_row(uint32_t E[16], uint32_t O[16], const fe &a, uint32_t bi, int i)
 {
-    uint32_t E[16], O[16];
+    // even p = i + j: j of the parity of i
+    const int je = i & 1;
+    E[i + je] = mad_lo_cc(a.v[je], bi, E[i + je]);
+    E[i + je + 1] = madc_hi_cc(a.v[je], bi, E[i + je + 1]);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) E[k] = O[k] = 0u;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const uint32_t bi = b.v[i];
-        // even p = i + j: j of the parity of i
-        const int je = i & 1;
-        E[i + je] = mad_lo_cc(a.v[je], bi, E[i + je]);
-        E[i + je + 1] = madc_hi_cc(a.v[je], bi, E[i + je + 1]);
-#pragma unroll
-        for (int j = je + 2; j < 8; j += 2) {
-            E[i + j] = madc_lo_cc(a.v[j], bi, E[i + j]);
-            E[i + j + 1] = madc_hi_cc(a.v[j], bi, E[i + j + 1]);
-        }
-        // the row's last window ends at E[i + je + 7]; the carry goes one
-        // word up (a word only carries have reached so far; E < 2^512, so
-        // past E[15] it is zero)
-        if (i + je + 8 < 16) E[i + je + 8] = addc(E[i + je + 8], 0u);
-        // odd p = i + j: j of the other parity, window at O[p - 1]
-        const int jo = je ^ 1;
-        O[i + jo - 1] = mad_lo_cc(a.v[jo], bi, O[i + jo - 1]);
-        O[i + jo] = madc_hi_cc(a.v[jo], bi, O[i + jo]);
-#pragma unroll
-        for (int j = jo + 2; j < 8; j += 2) {
-            O[i + j - 1] = madc_lo_cc(a.v[j], bi, O[i + j - 1]);
-            O[i + j] = madc_hi_cc(a.v[j], bi, O[i + j]);
-        }
-        if (i + jo + 7 < 16) O[i + jo + 7] = addc(O[i + jo + 7], 0u);
+    for (int j = je + 2; j < 8; j += 2) {
+        E[i + j] = madc_lo_cc(a.v[j], bi, E[i + j]);
+        E[i + j + 1] = madc_hi_cc(a.v[j], bi, E[i + j + 1]);
     }
-    // t = E + O * 2^32 (O[15] is zero: its weight is 2^512)
+    // the row's last window ends at E[i + je + 7]; the carry goes one
+    // word up (a word only carries have reached so far; E < 2^512, so
+    // past E[15] it is zero)
+    if (i + je + 8 < 16) E[i + je + 8] = addc(E[i + je + 8], 0u);
+    // odd p = i + j: j of the other parity, window at O[p - 1]
+    const int jo = je ^ 1;
+    O[i + jo - 1] = mad_lo_cc(a.v[jo], bi, O[i + jo - 1]);
+    O[i + jo] = madc_hi_cc(a.v[jo], bi, O[i + jo]);
+#pragma unroll
+    for (int j = jo + 2; j < 8; j += 2) {
+        O[i + j - 1] = madc_lo_cc(a.v[j], bi, O[i + j - 1]);
+        O[i + j] = madc_hi_cc(a.v[j], bi, O[i + j]);
+    }
+    if (i + jo + 7 < 16) O[i + jo + 7] = addc(O[i + jo + 7], 0u);
+}
+
+// t = E + O * 2^32 (O[15] is zero: its weight is 2^512)
+FT_DEV void mul_merge(uint32_t t[16], const uint32_t E[16], const uint32_t O[16])
+{
     t[0] = E[0];
     t[1] = add_cc(E[1], O[0]);
 #pragma unroll
     for (int k = 2; k < 15; ++k) t[k] = addc_cc(E[k], O[k - 1]);
     t[15] = addc(E[15], O[14]);
 }
-#else
-// t = a * b (full 512-bit product).  Operand scanning with each row split
-// by the parity of the multiplicand limb: products a_j * b_i with j even are
-// chained into T as (lo, hi) pairs of the same product, j odd into U, and
-// T + U is added at the end.  Keeping both halves of one product adjacent in
-// a chain lets ptxas fuse them: 237 SASS instructions per multiplication on
-// sm_103a against 300 for row-by-row lo-then-hi chains (measured).
+
 FT_DEV void mul_wide(uint32_t t[16], const fe &a, const fe &b)
 {
-    uint32_t T[16], U[16];
+    uint32_t E[16], O[16];
 #pragma unroll
-    for (int j = 0; j < 8; j += 2) {
-        T[j] = mul_lo(a.v[j], b.v[0]);
-        T[j + 1] = mul_hi(a.v[j], b.v[0]);
-        U[j + 1] = mul_lo(a.v[j + 1], b.v[0]);
-        U[j + 2] = mul_hi(a.v[j + 1], b.v[0]);
-    }
-    T[8] = 0u;
-    U[0] = 0u;
+    for (int k = 0; k < 16; ++k) E[k] = O[k] = 0u;
 #pragma unroll
-    for (int k = 9; k < 16; ++k) T[k] = U[k] = 0u;
-#pragma unroll
-    for (int i = 1; i < 8; ++i) {
-        T[i] = mad_lo_cc(a.v[0], b.v[i], T[i]);
-        T[i + 1] = madc_hi_cc(a.v[0], b.v[i], T[i + 1]);
-#pragma unroll
-        for (int j = 2; j < 8; j += 2) {
-            T[i + j] = madc_lo_cc(a.v[j], b.v[i], T[i + j]);
-            T[i + j + 1] = madc_hi_cc(a.v[j], b.v[i], T[i + j + 1]);
-        }
-        T[i + 8] = addc(T[i + 8], 0u);
-        U[i + 1] = mad_lo_cc(a.v[1], b.v[i], U[i + 1]);
-        U[i + 2] = madc_hi_cc(a.v[1], b.v[i], U[i + 2]);
-#pragma unroll
-        for (int j = 3; j < 8; j += 2) {
-            U[i + j] = madc_lo_cc(a.v[j], b.v[i], U[i + j]);
-            U[i + j + 1] = madc_hi_cc(a.v[j], b.v[i], U[i + j + 1]);
-        }
-        // the row's carry out of U[15] is zero: the partial product fits
-        if (i + 9 < 16) U[i + 9] = addc(U[i + 9], 0u);
-    }
-    t[0] = T[0];
-    t[1] = add_cc(T[1], U[1]);
-#pragma unroll
-    for (int k = 2; k < 15; ++k) t[k] = addc_cc(T[k], U[k]);
-    t[15] = addc(T[15], U[15]);
+    for (int i = 0; i < 8; ++i) mul_row(E, O, a, b.v[i], i);
+    mul_merge(t, E, O);
 }
-#endif
 
-#if FT_MUL_ALIGNED
+// two independent products with their rows interleaved (four carry chains
+// in flight instead of two)
+FT_DEV void mul_wide2(uint32_t t1[16], const fe &a1, const fe &b1, uint32_t t2[16], const fe &a2, const fe &b2)
+{
+    uint32_t E1[16], O1[16], E2[16], O2[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) E1[k] = O1[k] = E2[k] = O2[k] = 0u;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        mul_row(E1, O1, a1, b1.v[i], i);
+        mul_row(E2, O2, a2, b2.v[i], i);
+    }
+    mul_merge(t1, E1, O1);
+    mul_merge(t2, E2, O2);
+}
+
 // t = a^2: the 28 cross products a_i a_j (i < j) as 64-bit windows in even
 // aligned register pairs, as in mul_wide: even p = i + j in T (T[p],
 // T[p + 1]), odd p in O one word lower (O[p - 1], O[p]); row i chains its
 // products of each parity.  t = 2 (T + O * 2^32) + the 8 squares a_i^2,
 // whose windows (2i, 2i + 1) form one chain.
-FT_DEV void sqr_wide(uint32_t t[16], const fe &a)
+FT_DEV void sqr_row(uint32_t T[16], uint32_t O[16], const fe &a, int i)
 {
-    uint32_t T[16], O[16];
+    // j = i+1, i+3, ...: odd p, window at O[p - 1]
+    O[2 * i] = mad_lo_cc(a.v[i], a.v[i + 1], O[2 * i]);
+    O[2 * i + 1] = madc_hi_cc(a.v[i], a.v[i + 1], O[2 * i + 1]);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) T[k] = O[k] = 0u;
-#pragma unroll
-    for (int i = 0; i < 7; ++i) {
-        // j = i+1, i+3, ...: odd p, window at O[p - 1]
-        O[2 * i] = mad_lo_cc(a.v[i], a.v[i + 1], O[2 * i]);
-        O[2 * i + 1] = madc_hi_cc(a.v[i], a.v[i + 1], O[2 * i + 1]);
-#pragma unroll
-        for (int j = i + 3; j < 8; j += 2) {
-            O[i + j - 1] = madc_lo_cc(a.v[i], a.v[j], O[i + j - 1]);
-            O[i + j] = madc_hi_cc(a.v[i], a.v[j], O[i + j]);
-        }
-        {
-            const int last = i + 1 + 2 * ((6 - i) / 2);
-            if (i + last + 2 < 16) O[i + last + 1] = addc(O[i + last + 1], 0u);
-        }
-        // j = i+2, i+4, ...: even p
-        if (i < 6) {
-            T[2 * i + 2] = mad_lo_cc(a.v[i], a.v[i + 2], T[2 * i + 2]);
-            T[2 * i + 3] = madc_hi_cc(a.v[i], a.v[i + 2], T[2 * i + 3]);
-#pragma unroll
-            for (int j = i + 4; j < 8; j += 2) {
-                T[i + j] = madc_lo_cc(a.v[i], a.v[j], T[i + j]);
-                T[i + j + 1] = madc_hi_cc(a.v[i], a.v[j], T[i + j + 1]);
-            }
-            const int last = i + 2 + 2 * ((5 - i) / 2);
-            if (i + last + 2 < 16) T[i + last + 2] = addc(T[i + last + 2], 0u);
-        }
+    for (int j = i + 3; j < 8; j += 2) {
+        O[i + j - 1] = madc_lo_cc(a.v[i], a.v[j], O[i + j - 1]);
+        O[i + j] = madc_hi_cc(a.v[i], a.v[j], O[i + j]);
     }
+    {
+        const int last = i + 1 + 2 * ((6 - i) / 2);
+        if (i + last + 2 < 16) O[i + last + 1] = addc(O[i + last + 1], 0u);
+    }
+    // j = i+2, i+4, ...: even p
+    if (i < 6) {
+        T[2 * i + 2] = mad_lo_cc(a.v[i], a.v[i + 2], T[2 * i + 2]);
+        T[2 * i + 3] = madc_hi_cc(a.v[i], a.v[i + 2], T[2 * i + 3]);
+#pragma unroll
+        for (int j = i + 4; j < 8; j += 2) {
+            T[i + j] = madc_lo_cc(a.v[i], a.v[j], T[i + j]);
+            T[i + j + 1] = madc_hi_cc(a.v[i], a.v[j], T[i + j + 1]);
+        }
+        const int last = i + 2 + 2 * ((5 - i) / 2);
+        if (i + last + 2 < 16) T[i + last + 2] = addc(T[i + last + 2], 0u);
+    }
+}
+
+// t = 2 (T + O * 2^32) + the squares a_i^2
+FT_DEV void sqr_finish(uint32_t t[16], const uint32_t T[16], const uint32_t O[16], const fe &a)
+{
     // the cross products sum to less than a^2 / 2 < 2^511: no carry out
     uint32_t c[16];
     c[0] = T[0];
@@ -317,62 +259,31 @@ FT_DEV void sqr_wide(uint32_t t[16], const fe &a)
         t[2 * i + 1] = madc_hi_cc(a.v[i], a.v[i], t[2 * i + 1]);
     }
 }
-#else
-// t = a^2: the 28 cross products a_i a_j (i < j) are chained as (lo, hi)
-// pairs of the same product, split by the parity of i + j as in mul_wide
-// (even into T, odd into U); t = 2 (T + U) + the 8 squares, which form one
-// (lo, hi) chain.  Measured on sm_103a: 21% more squarings per second than
-// row-by-row lo-then-hi chains.
+
 FT_DEV void sqr_wide(uint32_t t[16], const fe &a)
 {
-    uint32_t T[16], U[16];
+    uint32_t T[16], O[16];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) T[k] = U[k] = 0u;
+    for (int k = 0; k < 16; ++k) T[k] = O[k] = 0u;
 #pragma unroll
-    for (int i = 0; i < 7; ++i) {
-        // j = i+1, i+3, ...: products whose low half lands at an odd position
-        U[2 * i + 1] = mad_lo_cc(a.v[i], a.v[i + 1], U[2 * i + 1]);
-        U[2 * i + 2] = madc_hi_cc(a.v[i], a.v[i + 1], U[2 * i + 2]);
-#pragma unroll
-        for (int j = i + 3; j < 8; j += 2) {
-            U[i + j] = madc_lo_cc(a.v[i], a.v[j], U[i + j]);
-            U[i + j + 1] = madc_hi_cc(a.v[i], a.v[j], U[i + j + 1]);
-        }
-        {
-            const int last = i + 1 + 2 * ((6 - i) / 2);
-            if (i + last + 2 < 16) U[i + last + 2] = addc(U[i + last + 2], 0u);
-        }
-        // j = i+2, i+4, ...: low half at an even position
-        if (i < 6) {
-            T[2 * i + 2] = mad_lo_cc(a.v[i], a.v[i + 2], T[2 * i + 2]);
-            T[2 * i + 3] = madc_hi_cc(a.v[i], a.v[i + 2], T[2 * i + 3]);
-#pragma unroll
-            for (int j = i + 4; j < 8; j += 2) {
-                T[i + j] = madc_lo_cc(a.v[i], a.v[j], T[i + j]);
-                T[i + j + 1] = madc_hi_cc(a.v[i], a.v[j], T[i + j + 1]);
-            }
-            const int last = i + 2 + 2 * ((5 - i) / 2);
-            if (i + last + 2 < 16) T[i + last + 2] = addc(T[i + last + 2], 0u);
-        }
-    }
-    // the cross products sum to less than a^2 / 2 < 2^511: no carry out
-    uint32_t c[16];
-    c[0] = add_cc(T[0], U[0]);
-#pragma unroll
-    for (int k = 1; k < 16; ++k) c[k] = addc_cc(T[k], U[k]);
-    t[0] = add_cc(c[0], c[0]);
-#pragma unroll
-    for (int k = 1; k < 16; ++k) t[k] = addc_cc(c[k], c[k]);
-    t[0] = mad_lo_cc(a.v[0], a.v[0], t[0]);
-    t[1] = madc_hi_cc(a.v[0], a.v[0], t[1]);
-#pragma unroll
-    for (int i = 1; i < 8; ++i) {
-        t[2 * i] = madc_lo_cc(a.v[i], a.v[i], t[2 * i]);
-        t[2 * i + 1] = madc_hi_cc(a.v[i], a.v[i], t[2 * i + 1]);
-    }
+    for (int i = 0; i < 7; ++i) sqr_row(T, O, a, i);
+    sqr_finish(t, T, O, a);
 }
 
-#endif
+// two independent squarings with their rows interleaved
+FT_DEV void sqr_wide2(uint32_t t1[16], const fe &a1, uint32_t t2[16], const fe &a2)
+{
+    uint32_t T1[16], O1[16], T2[16], O2[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) T1[k] = O1[k] = T2[k] = O2[k] = 0u;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        sqr_row(T1, O1, a1, i);
+        sqr_row(T2, O2, a2, i);
+    }
+    sqr_finish(t1, T1, O1, a1);
+    sqr_finish(t2, T2, O2, a2);
+}
 
 FT_DEV void fe_mul(fe &h, const fe &a, const fe &b)
 {
@@ -386,6 +297,24 @@ FT_DEV void fe_sq(fe &h, const fe &a)
     uint32_t t[16];
     sqr_wide(t, a);
     fe_fold512(h, t);
+}
+
+// h1 = a1 b1 and h2 = a2 b2, interleaved (the outputs may alias the inputs)
+FT_DEV void fe_mul_x2(fe &h1, const fe &a1, const fe &b1, fe &h2, const fe &a2, const fe &b2)
+{
+    uint32_t t1[16], t2[16];
+    mul_wide2(t1, a1, b1, t2, a2, b2);
+    fe_fold512(h1, t1);
+    fe_fold512(h2, t2);
+}
+
+// h1 = a1^2 and h2 = a2^2, interleaved (the outputs may alias the inputs)
+FT_DEV void fe_sq_x2(fe &h1, const fe &a1, fe &h2, const fe &a2)
+{
+    uint32_t t1[16], t2[16];
+    sqr_wide2(t1, a1, t2, a2);
+    fe_fold512(h1, t1);
+    fe_fold512(h2, t2);
 }
 
 // 2 * a^2 (fe25519_sq2, sodium_fe.cu:1109)

@@ -10,6 +10,13 @@
 #pragma once
 #include "fe.cuh"
 
+// FT_MUL_PAIRS: independent multiplications (and squarings) of a formula
+// are computed two at a time with their rows interleaved (fe_mul_x2,
+// fe_sq_x2); the same products, so the same values.
+#ifndef FT_MUL_PAIRS
+#define FT_MUL_PAIRS 0
+#endif
+
 struct ge_p2 { fe X, Y, Z; };
 struct ge_p3 { fe X, Y, Z, T; };
 struct ge_p1p1 { fe X, Y, Z, T; };
@@ -26,10 +33,15 @@ FT_DEV void ge_add(ge_p1p1 &r, const ge_p3 &p, const ge_cached &q)
     fe t0;
     fe_add(r.X, p.Y, p.X);
     fe_sub(r.Y, p.Y, p.X);
+#if FT_MUL_PAIRS
+    fe_mul_x2(r.Z, r.X, q.YplusX, r.Y, r.Y, q.YminusX);
+    fe_mul_x2(r.T, q.T2d, p.T, r.X, p.Z, q.Z);
+#else
     fe_mul(r.Z, r.X, q.YplusX);
     fe_mul(r.Y, r.Y, q.YminusX);
     fe_mul(r.T, q.T2d, p.T);
     fe_mul(r.X, p.Z, q.Z);
+#endif
     fe_add(t0, r.X, r.X);
     fe_sub(r.X, r.Z, r.Y);
     fe_add(r.Y, r.Z, r.Y);
@@ -60,8 +72,12 @@ FT_DEV void ge_madd(ge_p1p1 &r, const ge_p3 &p, const ge_precomp &q)
     fe t0;
     fe_add(r.X, p.Y, p.X);
     fe_sub(r.Y, p.Y, p.X);
+#if FT_MUL_PAIRS
+    fe_mul_x2(r.Z, r.X, q.yplusx, r.Y, r.Y, q.yminusx);
+#else
     fe_mul(r.Z, r.X, q.yplusx);
     fe_mul(r.Y, r.Y, q.yminusx);
+#endif
     fe_mul(r.T, q.xy2d, p.T);
     fe_add(t0, p.Z, p.Z);
     fe_sub(r.X, r.Z, r.Y);
@@ -72,28 +88,44 @@ FT_DEV void ge_madd(ge_p1p1 &r, const ge_p3 &p, const ge_precomp &q)
 
 FT_DEV void ge_p1p1_to_p2(ge_p2 &r, const ge_p1p1 &p) // sodium_ge.cu:273
 {
+#if FT_MUL_PAIRS
+    fe_mul_x2(r.X, p.X, p.T, r.Y, p.Y, p.Z);
+#else
     fe_mul(r.X, p.X, p.T);
     fe_mul(r.Y, p.Y, p.Z);
+#endif
     fe_mul(r.Z, p.Z, p.T);
 }
 
 FT_DEV void ge_p1p1_to_p3(ge_p3 &r, const ge_p1p1 &p) // sodium_ge.cu:285
 {
+#if FT_MUL_PAIRS
+    fe_mul_x2(r.X, p.X, p.T, r.Y, p.Y, p.Z);
+    fe_mul_x2(r.Z, p.Z, p.T, r.T, p.X, p.Y);
+#else
     fe_mul(r.X, p.X, p.T);
     fe_mul(r.Y, p.Y, p.Z);
     fe_mul(r.Z, p.Z, p.T);
     fe_mul(r.T, p.X, p.Y);
+#endif
 }
 
 // r = 2p  (ge25519_p2_dbl, sodium_ge.cu:306-320)
 FT_DEV void ge_p2_dbl(ge_p1p1 &r, const ge_p2 &p)
 {
     fe t0;
+#if FT_MUL_PAIRS
+    fe_sq_x2(r.X, p.X, r.Z, p.Y);
+    fe_add(r.Y, p.X, p.Y);
+    fe_sq_x2(r.T, p.Z, t0, r.Y);
+    fe_add(r.T, r.T, r.T); // fe_sq2
+#else
     fe_sq(r.X, p.X);
     fe_sq(r.Z, p.Y);
     fe_sq2(r.T, p.Z);
     fe_add(r.Y, p.X, p.Y);
     fe_sq(t0, r.Y);
+#endif
     fe_add(r.Y, r.Z, r.X);
     fe_sub(r.Z, r.Z, r.X);
     fe_sub(r.X, t0, r.Y);

@@ -107,6 +107,14 @@ FT_DEV void ge_add_select(ge_p1p1 &r, const ge_p3 &p, const Tab &tab, int d)
     }
     fe_add(r.X, p.Y, p.X);
     fe_sub(r.Y, p.Y, p.X);
+#if FT_MUL_PAIRS
+    fe_mul_x2(r.Z, r.X, a, r.Y, r.Y, b);
+    tab.template select_fe<NE>(a, 3, babs, false);
+    fe_neg(b, a); // -P negates T2d
+    fe_cmov(a, b, nm);
+    tab.template select_fe<NE>(b, 2, babs, true);
+    fe_mul_x2(r.T, a, p.T, r.X, p.Z, b);
+#else
     fe_mul(r.Z, r.X, a);
     fe_mul(r.Y, r.Y, b);
     tab.template select_fe<NE>(a, 3, babs, false);
@@ -115,6 +123,7 @@ FT_DEV void ge_add_select(ge_p1p1 &r, const ge_p3 &p, const Tab &tab, int d)
     fe_mul(r.T, a, p.T);
     tab.template select_fe<NE>(a, 2, babs, true);
     fe_mul(r.X, p.Z, a);
+#endif
     fe_add(t0, r.X, r.X);
     fe_sub(r.X, r.Z, r.Y);
     fe_add(r.Y, r.Z, r.Y);
