@@ -160,9 +160,8 @@ cudaError_t d2h(void *dst, const void *src, size_t bytes, cudaStream_t st = null
 // Marks that the work just queued on the library stream completes a's
 // writes: an export of a that follows, with no other use of a in between,
 // waits for this point only (export_begin), not for everything queued after.
-cudaError_t mark_ready(const_ft_ge25519_array ca)
+cudaError_t mark_ready(ft_ge25519_array a)
 {
-    auto *a = const_cast<ft_ge25519_array_s *>(ca);
     if (a->exposed.load()) return cudaSuccess;
     if (!a->ready) {
         cudaError_t e = cudaEventCreateWithFlags(&a->ready, cudaEventDisableTiming);
