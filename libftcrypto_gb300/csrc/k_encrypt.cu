@@ -44,6 +44,28 @@ FT_DEV void enc_put(uint4 *dst, size_t s, size_t i, const ge_p3 &h)
     }
 }
 
+#ifndef FT_ENC_RELOAD
+#define FT_ENC_RELOAD 0
+#endif
+
+// the radix-32 digits (biased) of the 32-byte scalar r[i], as the reference
+// effectively uses it (enc_ref_scalar)
+FT_DEV void enc_r_digits(uint32_t c[9], const uint4 *r, size_t i)
+{
+    const uint4 s0 = r[2 * i], s1v = r[2 * i + 1];
+    const uint32_t a[8] = {s0.x, s0.y, s0.z, s0.w, s1v.x, s1v.y, s1v.z, s1v.w};
+    uint32_t ar[8];
+    enc_ref_scalar(ar, a);
+    enc_recode(c, ar, ENC_ROWS);
+}
+
+// the first mdig biased digits of a 64-bit value (m + its bias < 2^70)
+FT_DEV void enc_m_digits(uint32_t c[9], uint64_t mv, int mdig)
+{
+    const uint32_t a[8] = {(uint32_t)mv, (uint32_t)(mv >> 32), 0u, 0u, 0u, 0u, 0u, 0u};
+    enc_recode(c, a, mdig);
+}
+
 template <bool ACC>
 __global__ void __launch_bounds__(ENC_NT, 1) k_encrypt(uint4 *c1, size_t s1, uint4 *c2, size_t s2, size_t n,
                                                       const uint4 *r, const uint64_t *m, int mdig,
@@ -55,6 +77,29 @@ __global__ void __launch_bounds__(ENC_NT, 1) k_encrypt(uint4 *c1, size_t s1, uin
     const uint4 *tb = smem, *tp = smem + ENC_TABLE_U4;
     FT_GRID_LOOP(i, n)
     {
+#if FT_ENC_RELOAD
+        // the digits of r and m are recoded again from global memory where
+        // their rows start, instead of being kept in 12 registers for it
+        uint32_t c[9];
+        enc_r_digits(c, r, i);
+        ge_p3 h;
+        ge_p3_0(h);
+        const int nrows = 2 * ENC_ROWS + mdig;
+#pragma unroll 1
+        for (int t = 0; t < nrows; ++t) {
+            if (t == ENC_ROWS) {
+                enc_put<ACC>(c1, s1, i, h);
+                ge_p3_0(h);
+                enc_r_digits(c, r, i);
+            } else if (t == 2 * ENC_ROWS) {
+                enc_m_digits(c, ACC ? 0 : m[i], mdig);
+            }
+            const int row = t < ENC_ROWS ? t : (t < 2 * ENC_ROWS ? t - ENC_ROWS : t - 2 * ENC_ROWS);
+            const uint4 *tab = (t >= ENC_ROWS && t < 2 * ENC_ROWS) ? tp : tb;
+            enc_comb_row(h, c, tab + (size_t)row * ENC_ENTRIES * 6);
+        }
+        enc_put<ACC>(c2, s2, i, h);
+#else
         uint32_t br[9], bm[3], c[9];
         {
             const uint4 s0 = r[2 * i], s1v = r[2 * i + 1];
@@ -98,6 +143,7 @@ __global__ void __launch_bounds__(ENC_NT, 1) k_encrypt(uint4 *c1, size_t s1, uin
             enc_comb_row(h, c, tab + (size_t)row * ENC_ENTRIES * 6);
         }
         enc_put<ACC>(c2, s2, i, h);
+#endif
     }
 }
 

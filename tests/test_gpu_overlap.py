@@ -145,3 +145,28 @@ def test_pinned_scalar_staging_ring(ft, orc):
         wants.append(orc.mul(orc.mul(orc.mul(p, k1, threads=8), k2, threads=8), k1, threads=8))
     for a, w in zip(arrs, wants):
         assert (a.to_bytes_folded() == orc.encode(w, 8)).all()
+
+
+def test_server_write_after_mark_is_seen(ft, orc):
+    """c1, c2 marked by ft_mul, then multiplied in place by a server request
+    (on the server's own stream): once the request's result is taken, the
+    exports show the server's product, not the marked state."""
+    g = synth.rng(76)
+    n = 2500
+    p1 = orc.from_scalars(synth.scalars_mod_L(g, n), threads=8)
+    p2 = orc.from_scalars(synth.scalars_mod_L(g, n), threads=8)
+    k1 = synth.scalars_mod_L(g, n)
+    k2 = synth.scalars_mod_L(g, n)
+    c1, c2 = ft.Array.from_packed(p1), ft.Array.from_packed(p2)
+    c1.mul(k1)
+    c2.mul(k1)
+    sk = synth.scalars_mod_L(g, 1)
+    pk = ft.Array.from_scalars(sk).to_bytes_folded()[0]
+    srv = ft.Server(pk, 1 << 30, slots=2)
+    try:
+        t = srv.submit_smul(c1, c2, k2)
+        srv.wait(t)
+        assert (c1.to_bytes_folded() == orc.encode(orc.mul(orc.mul(p1, k1, threads=8), k2, threads=8), 8)).all()
+        assert (c2.to_bytes_folded() == orc.encode(orc.mul(orc.mul(p2, k1, threads=8), k2, threads=8), 8)).all()
+    finally:
+        srv.close()
