@@ -27,22 +27,8 @@ FT_DEV void load_scalar(uint32_t a[8], const uint4 *sc, size_t i)
 
 
 
-// FT_LADDER_SMEM_DIGITS: the TMEM kernel keeps each thread's biased scalar
-// in shared memory (32 bytes per thread after the tables) rather than in 8
-// registers.
-#ifndef FT_LADDER_SMEM_DIGITS
-#define FT_LADDER_SMEM_DIGITS 0
-#endif
-
-// (only where the 32 bytes per thread fit beside the tables: NT = 384, not 448)
 template <int NT>
-constexpr bool kLadderSmemDigits = FT_LADDER_SMEM_DIGITS && NT > 256 && (size_t)NT * (4 * 8 * 16 + 32) <= 227 * 1024;
-
-template <int NT>
-constexpr size_t ladder_smem_bytes()
-{
-    return (size_t)NT * (NT > 256 ? 4 : 8) * 8 * sizeof(uint4) + (kLadderSmemDigits<NT> ? (size_t)NT * 32 : 0);
-}
+constexpr size_t ladder_smem_bytes() { return (size_t)NT * (NT > 256 ? 4 : 8) * 8 * sizeof(uint4); }
 
 template <int NT>
 __global__ void __launch_bounds__(NT, 1) k_smul_var(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step)
@@ -99,12 +85,7 @@ __global__ void __maxnreg__(tm_max_regs<NT>()) k_smul_var_tm(uint4 *p, size_t s,
     __syncwarp();
     smul_build_table(tab, P);
     tmem_wait_st();
-    if constexpr (kLadderSmemDigits<NT>) {
-        uint32_t *sdig = reinterpret_cast<uint32_t *>(smem + (size_t)NT * 4 * 8) + threadIdx.x;
-        smul_ladder<HybridTab<NT>, true>(h, a, tab, true, sdig, NT); // every thread runs the whole ladder
-    } else {
-        smul_ladder(h, a, tab, true); // every thread runs the whole ladder
-    }
+    smul_ladder(h, a, tab, true); // every thread runs the whole ladder
     if (live) st_p3(p, s, i, h);
     tmem_sync_threads();
     if (warp == 0) tmem_free(s_taddr, 512u);
