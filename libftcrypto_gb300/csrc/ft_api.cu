@@ -170,8 +170,10 @@ cudaError_t mark_ready(ft_ge25519_array a)
             return e;
         }
     }
-    a->ready_touch = a->touch.load();
-    return cudaEventRecord(a->ready, g.stream);
+    const uint64_t t = a->touch.load();
+    const cudaError_t e = cudaEventRecord(a->ready, g.stream);
+    a->ready_touch = e == cudaSuccess ? t : UINT64_MAX; // a failed mark keeps exports in order
+    return e;
 }
 
 // The stream and the device buffer (at least `bytes`) an export of a

@@ -18,6 +18,10 @@
 #define FT_TAB_FN inline
 #endif
 
+#ifndef FT_TMEM_SEL_X8
+#define FT_TMEM_SEL_X8 0
+#endif
+
 namespace ft {
 
 template <int NT>
@@ -117,6 +121,17 @@ struct HybridTab {
         // (a select with some entries multiplied by 0/1 indicators on the
         // multiply-add pipe instead of masked measured 3% slower: the field
         // multiplications keep that pipe busy)
+#if FT_TMEM_SEL_X8
+        // one entry (8 columns) per load: 8 registers in flight, not 32
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            uint32_t r[8];
+            tmem_ld8(col + 32u * (uint32_t)j + 8u * (uint32_t)k, r);
+            const uint32_t m = ct_eq_mask(babs, (uint32_t)(k + 5));
+#pragma unroll
+            for (int w = 0; w < 8; ++w) f.v[w] ^= (f.v[w] ^ r[w]) & m;
+        }
+#else
         uint32_t r[32];
         tmem_ld32(col + 32u * (uint32_t)j, r);
 #pragma unroll
@@ -125,6 +140,7 @@ struct HybridTab {
 #pragma unroll
             for (int w = 0; w < 8; ++w) f.v[w] ^= (f.v[w] ^ r[8 * k + w]) & m;
         }
+#endif
     }
 };
 
