@@ -49,6 +49,7 @@ static inline uint32_t tmem_warp_addr(uint32_t base, int warp, uint32_t col)
 }
 static inline void tmem_st8(uint32_t ta, const uint32_t v[8]) { memcpy(tmem_cell(ta, 8), v, 32); }
 static inline void tmem_ld8(uint32_t ta, uint32_t r[8]) { memcpy(r, tmem_cell(ta, 8), 32); }
+static inline void tmem_ld16(uint32_t ta, uint32_t r[16]) { memcpy(r, tmem_cell(ta, 16), 64); }
 static inline void tmem_ld32(uint32_t ta, uint32_t r[32]) { memcpy(r, tmem_cell(ta, 32), 128); }
 static inline void tmem_wait_st() {}
 // one emulated thread at a time: a block barrier has nothing to wait for
