@@ -125,7 +125,8 @@ struct HybridTab {
         // FT_TMEM_SEL_COLS columns per load (8: one entry, 16: two, 32: all
         // four), each load waited for before its entries are merged.
         // Ladder of 1,048,576 points: 20.31 ms with one load of 32 columns
-        // (32 registers in flight), 20.19 ms with four of 8.
+        // (32 registers in flight), 20.24 ms with two of 16, 20.19 ms with
+        // four of 8.
         constexpr int EPL = FT_TMEM_SEL_COLS / 8; // entries per load
 #pragma unroll
         for (int k0 = 0; k0 < 4; k0 += EPL) {

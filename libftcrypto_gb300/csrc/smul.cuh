@@ -84,10 +84,6 @@ FT_DEV void tab_select_fe(fe &f, const Tab &tab, int j, uint32_t babs, bool one)
     }
 }
 
-#ifndef FT_SELECT_PAIRS
-#define FT_SELECT_PAIRS 1
-#endif
-
 // r = p + d * P for a signed digit d in [-NE, NE], where tab holds (k+1)*P:
 // the reference's cmov8_cached select (sodium_ge.cu:490-511) followed by
 // ge_add (the same field operations on the same
@@ -111,7 +107,7 @@ FT_DEV void ge_add_select(ge_p1p1 &r, const ge_p3 &p, const Tab &tab, int d)
     }
     fe_add(r.X, p.Y, p.X);
     fe_sub(r.Y, p.Y, p.X);
-#if FT_MUL_PAIRS && FT_SELECT_PAIRS
+#if FT_MUL_PAIRS
     fe_mul_x2(r.Z, r.X, a, r.Y, r.Y, b);
     tab.template select_fe<NE>(a, 3, babs, false);
     fe_neg(b, a); // -P negates T2d
