@@ -20,6 +20,9 @@
 #ifndef FT_MUL_PAIRS
 #define FT_MUL_PAIRS 1
 #endif
+#ifndef FT_SQ_PAIRS
+#define FT_SQ_PAIRS 1
+#endif
 
 struct ge_p2 { fe X, Y, Z; };
 struct ge_p3 { fe X, Y, Z, T; };
@@ -118,7 +121,7 @@ FT_DEV void ge_p1p1_to_p3(ge_p3 &r, const ge_p1p1 &p) // sodium_ge.cu:285
 FT_DEV void ge_p2_dbl(ge_p1p1 &r, const ge_p2 &p)
 {
     fe t0;
-#if FT_MUL_PAIRS
+#if FT_MUL_PAIRS && FT_SQ_PAIRS
     fe_sq_x2(r.X, p.X, r.Z, p.Y);
     fe_add(r.Y, p.X, p.Y);
     fe_sq_x2(r.T, p.Z, t0, r.Y);
