@@ -63,7 +63,10 @@ FT_DEV void shr5_288(uint32_t c[9])
 // fully unrolled and 13.96 with one (instruction fetch and load latency);
 // moving some entries to the multiply-add pipe (products by 0/1 indicators)
 // measured 1-3% slower at every grouping.
-static constexpr int ENC_SEL_GROUP = 4;
+#ifndef FT_ENC_SEL_GROUP
+#define FT_ENC_SEL_GROUP 4
+#endif
+static constexpr int ENC_SEL_GROUP = FT_ENC_SEL_GROUP;
 static_assert(ENC_ENTRIES % ENC_SEL_GROUP == 0, "select grouping");
 
 FT_DEV void enc_select(ge_precomp &t, int d, const uint4 *row)
