@@ -58,13 +58,15 @@ FT_DEV void shr5_288(uint32_t c[9])
 
 // t = the entry |d| of a table row (ENC_ENTRIES entries), negated for d < 0;
 // the identity for d = 0; every entry is read and merged under its mask.
-// Four entries per iteration of a rolled loop: 12.03 ms for the encryption
-// of 1,048,576 plaintexts, against 12.06 with two, 12.33 with eight, 12.71
-// fully unrolled and 13.96 with one (instruction fetch and load latency);
-// moving some entries to the multiply-add pipe (products by 0/1 indicators)
-// measured 1-3% slower at every grouping.
+// Eight entries per iteration of a rolled loop.  With the field arithmetic
+// of the time: 12.03 ms for the encryption of 1,048,576 plaintexts with
+// four, 12.06 with two, 12.33 with eight, 12.71 fully unrolled and 13.96
+// with one (instruction fetch and load latency); after the encryption
+// stopped keeping the digits of r and m in registers: 9.78 ms with four,
+// 9.90 with two, 9.72 with eight.  Moving some entries to the multiply-add
+// pipe (products by 0/1 indicators) measured 1-3% slower at every grouping.
 #ifndef FT_ENC_SEL_GROUP
-#define FT_ENC_SEL_GROUP 4
+#define FT_ENC_SEL_GROUP 8
 #endif
 static constexpr int ENC_SEL_GROUP = FT_ENC_SEL_GROUP;
 static_assert(ENC_ENTRIES % ENC_SEL_GROUP == 0, "select grouping");
