@@ -63,7 +63,7 @@ FT_DEV void shr5_288(uint32_t c[9])
 // four, 12.06 with two, 12.33 with eight, 12.71 fully unrolled and 13.96
 // with one (instruction fetch and load latency); after the encryption
 // stopped keeping the digits of r and m in registers: 9.78 ms with four,
-// 9.90 with two, 9.72 with eight.  Moving some entries to the multiply-add
+// 9.90 with two, 9.72 with eight or sixteen.  Moving some entries to the multiply-add
 // pipe (products by 0/1 indicators) measured 1-3% slower at every grouping.
 #ifndef FT_ENC_SEL_GROUP
 #define FT_ENC_SEL_GROUP 8
