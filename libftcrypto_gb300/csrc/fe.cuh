@@ -130,10 +130,6 @@ FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
     for (int k = 0; k < 8; ++k) h.v[k] = r[k];
 }
 
-#ifndef FT_MUL_SWAP
-#define FT_MUL_SWAP 0
-#endif
-
 // t = a * b (full 512-bit product).  Each product a_j * b_i is one 64-bit
 // window (lo at position p = i + j, hi at p + 1) that ptxas computes with
 // one IMAD.WIDE into an even-aligned register pair.  Windows at even p
@@ -147,35 +143,6 @@ FT_DEV void fe_fold512(fe &h, const uint32_t t[16])
 // Field-multiplication throughput of other schedules, measured: one level of
 // Karatsuba (48 products and ~55 more additions) 7.08 T products/s, four
 // independent 4 x 4 blocks 6.83, this one 7.89.
-#if FT_MUL_SWAP
-FT_DEV void mul_row(uint32_t E[16], uint32_t O[16], const fe &a, uint32_t bi, int i)
-{
-    // even p = i + j: j of the parity of i
-    const int je = i & 1;
-    E[i + je] = mad_lo_cc(bi, a.v[je], E[i + je]);
-    E[i + je + 1] = madc_hi_cc(bi, a.v[je], E[i + je + 1]);
-#pragma unroll
-    for (int j = je + 2; j < 8; j += 2) {
-        E[i + j] = madc_lo_cc(bi, a.v[j], E[i + j]);
-        E[i + j + 1] = madc_hi_cc(bi, a.v[j], E[i + j + 1]);
-    }
-    // the row's last window ends at E[i + je + 7]; the carry goes one
-    // word up (a word only carries have reached so far; E < 2^512, so
-    // past E[15] it is zero)
-    if (i + je + 8 < 16) E[i + je + 8] = addc(E[i + je + 8], 0u);
-    // odd p = i + j: j of the other parity, window at O[p - 1]
-    const int jo = je ^ 1;
-    O[i + jo - 1] = mad_lo_cc(bi, a.v[jo], O[i + jo - 1]);
-    O[i + jo] = madc_hi_cc(bi, a.v[jo], O[i + jo]);
-#pragma unroll
-    for (int j = jo + 2; j < 8; j += 2) {
-        O[i + j - 1] = madc_lo_cc(bi, a.v[j], O[i + j - 1]);
-        O[i + j] = madc_hi_cc(bi, a.v[j], O[i + j]);
-    }
-    if (i + jo + 7 < 16) O[i + jo + 7] = addc(O[i + jo + 7], 0u);
-}
-
-#else
 FT_DEV void mul_row(uint32_t E[16], uint32_t O[16], const fe &a, uint32_t bi, int i)
 {
     // even p = i + j: j of the parity of i
@@ -203,7 +170,6 @@ FT_DEV void mul_row(uint32_t E[16], uint32_t O[16], const fe &a, uint32_t bi, in
     if (i + jo + 7 < 16) O[i + jo + 7] = addc(O[i + jo + 7], 0u);
 }
 
-#endif
 // t = E + O * 2^32 (O[15] is zero: its weight is 2^512)
 FT_DEV void mul_merge(uint32_t t[16], const uint32_t E[16], const uint32_t O[16])
 {
