@@ -179,7 +179,7 @@ def profile_traffic():
 
 def imad_peak(sm_count: int):
     """32x32->64 products per second of the mad.wide.u32 probe alone
-    (libftbench.so; its ncu summary is profiles/k_imad_int_peaks.md)."""
+    (libftbench.so)."""
     import ctypes
     lib = ctypes.CDLL(os.path.join(ROOT, "libftcrypto_gb300", "libftbench.so"))
     lib.ftb_imad_wide_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
@@ -975,7 +975,7 @@ PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan",
 
 
 def run_profile(case: str, size: int | None = None) -> int:
-    """One small run of one kernel family, for ncu (profiles/*.md): inputs are
+    """One small run of one kernel family, for ncu captures: inputs are
     built, then the operation runs twice (the second launch is the one to
     capture with `-s <setup launches + 1> -c 1` or `-k regex:<kernel>`).
     `size` (--profile-n) sets the number of points (ciphertext halves for
