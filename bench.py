@@ -177,18 +177,6 @@ def profile_traffic():
 
 # ---------------------------------------------------------------- our arm
 
-def imad_peak(sm_count: int):
-    """32x32->64 products per second of the mad.wide.u32 probe alone
-    (libftbench.so)."""
-    import ctypes
-    lib = ctypes.CDLL(os.path.join(ROOT, "libftcrypto_gb300", "libftbench.so"))
-    lib.ftb_imad_wide_peak.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
-    v = ctypes.c_double(0)
-    if lib.ftb_imad_wide_peak(ctypes.byref(v), sm_count) != 0:
-        return None
-    return v.value
-
-
 def int_peaks(sm_count: int, gpu_index: int, seconds: float = 1.5):
     """The integer-pipe probes of libftbench.so (csrc/bench_peak.cu), repeated
     for `seconds` while nvidia-smi samples the SM clock; best of all runs, in

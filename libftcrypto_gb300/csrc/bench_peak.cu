@@ -135,12 +135,3 @@ extern "C" int ftb_int_peaks(double *out, int sm_count, int reps)
     out[2] = (double)mul_blocks * 128 * mul_iters * 2 * 64 / (ms_mul * 1e-3);
     return 0;
 }
-
-// the first probe alone (bench.py's roofline peak)
-extern "C" int ftb_imad_wide_peak(double *products_per_s, int sm_count)
-{
-    double v[3];
-    int rc = ftb_int_peaks(v, sm_count, 5);
-    if (rc == 0) *products_per_s = v[0];
-    return rc;
-}
