@@ -958,7 +958,8 @@ def run_ours(args):
     return 0
 
 
-PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan", "ct_scan", "segsum", "isum", "encode",
+PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan", "ct_scan", "segsum", "isum",
+                 "isum_one_key", "encode",
                  "decode", "batch", "export", "int_peaks")
 
 
@@ -999,7 +1000,7 @@ def run_profile(case: str, size: int | None = None) -> int:
         op = lambda: ft.encrypt_device(c1, c2, pk, m.data_ptr(), d_sc.data_ptr(), n, 8)  # noqa: E731
     elif case == "comb":
         op = lambda: ft.Array.from_scalars(sc)  # noqa: E731
-    elif case in ("add", "reduce", "scan", "ct_scan", "segsum", "isum"):
+    elif case in ("add", "reduce", "scan", "ct_scan", "segsum", "isum", "isum_one_key"):
         big = size or (1 << 24 if case in ("reduce", "segsum") else 1 << 22)
         a = ft.Array.init_point(big, base, 3)
         a.add(ft.Array.init_point(big, base, 5))
@@ -1020,9 +1021,13 @@ def run_profile(case: str, size: int | None = None) -> int:
             torch.cuda.synchronize()
             out = ft.Array.init_scalar(big // 16)
             op = lambda: ft.segmented_sum_csr_device(out, d_off.data_ptr(), big // 16, a)  # noqa: E731
-        else:
+        elif case == "isum":
             keys = g.integers(0, big // 16, big).astype(np.uint64)
             res = ft.Array.init_scalar(big // 16)
+            op = lambda: res.reduce_isum(keys, a)  # noqa: E731
+        else:  # every key equal: one segment of all the points (the prefix-difference path)
+            keys = np.full(big, 3, np.uint64)
+            res = ft.Array.init_scalar(8)
             op = lambda: res.reduce_isum(keys, a)  # noqa: E731
     elif case == "ct_add":  # two arrays of 1,048,576 ciphertexts (1 GB: larger than L2)
         c1, c2, d1, d2 = (ft.Array.init_point(n, base, k) for k in (3, 5, 7, 9))
