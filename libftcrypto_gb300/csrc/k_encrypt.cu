@@ -62,39 +62,53 @@ FT_DEV void enc_m_digits(uint32_t c[9], uint64_t mv, int mdig)
     enc_recode(c, a, mdig);
 }
 
+#ifndef FT_ENC_SPLIT
+#define FT_ENC_SPLIT 1
+#endif
+
+// Work units: half 0 of ciphertext i is c1 = r*B (52 rows of B's table),
+// half 1 is c2 = r*PK + m*B (52 rows of the key's table, then mdig rows of
+// B's).  With `split` the 2n halves are spread over the grid as separate
+// units (a thread takes units u, u + threads, ...): 2n units make the
+// last wave of the grid-stride loop fuller than n whole ciphertexts, whose
+// last wave kept about half the threads idle (1,048,576 ciphertexts over
+// 152 x 512 threads: 13.47 per thread).  Without it (c1 and c2 the same
+// array, so its two halves must run in order in one thread) a thread takes
+// both halves of each of its ciphertexts.
 template <bool ACC>
 __global__ void __launch_bounds__(ENC_NT, 1) k_encrypt(uint4 *c1, size_t s1, uint4 *c2, size_t s2, size_t n,
                                                       const uint4 *r, const uint64_t *m, int mdig,
-                                                      const uint4 *tables)
+                                                      const uint4 *tables, int split)
 {
     extern __shared__ uint4 smem[];
     for (size_t j = threadIdx.x; j < 2 * ENC_TABLE_U4; j += ENC_NT) smem[j] = tables[j];
     __syncthreads();
     const uint4 *tb = smem, *tp = smem + ENC_TABLE_U4;
-    FT_GRID_LOOP(i, n)
+    const size_t units = split ? 2 * n : n;
+    FT_GRID_LOOP(u, units)
     {
-        // the digits of r and m are recoded from global memory where their
-        // rows start, rather than kept in 12 registers from the start (128
-        // registers with 32 bytes of spills before; 9.79 -> 9.77 ms)
-        uint32_t c[9];
-        enc_r_digits(c, r, i);
-        ge_p3 h;
-        ge_p3_0(h);
-        const int nrows = 2 * ENC_ROWS + mdig;
+        const size_t i = split && u >= n ? u - n : u;
+        const int h0 = split && u >= n ? 1 : 0, h1 = split ? h0 : 1;
 #pragma unroll 1
-        for (int t = 0; t < nrows; ++t) {
-            if (t == ENC_ROWS) {
-                enc_put<ACC>(c1, s1, i, h);
-                ge_p3_0(h);
-                enc_r_digits(c, r, i);
-            } else if (t == 2 * ENC_ROWS) {
-                enc_m_digits(c, ACC ? 0 : m[i], mdig);
+        for (int half = h0; half <= h1; ++half) {
+            // the digits of r and m are recoded from global memory where
+            // their rows start, rather than kept in 12 registers throughout
+            // (128 registers with 32 bytes of spills before; 9.79 -> 9.77 ms)
+            uint32_t c[9];
+            enc_r_digits(c, r, i);
+            ge_p3 h;
+            ge_p3_0(h);
+            const int nrows = half ? ENC_ROWS + mdig : ENC_ROWS;
+#pragma unroll 1
+            for (int t = 0; t < nrows; ++t) {
+                if (t == ENC_ROWS) enc_m_digits(c, ACC ? 0 : m[i], mdig);
+                const int row = t < ENC_ROWS ? t : t - ENC_ROWS;
+                const uint4 *tab = (half && t < ENC_ROWS) ? tp : tb;
+                enc_comb_row(h, c, tab + (size_t)row * ENC_ENTRIES * 6);
             }
-            const int row = t < ENC_ROWS ? t : (t < 2 * ENC_ROWS ? t - ENC_ROWS : t - 2 * ENC_ROWS);
-            const uint4 *tab = (t >= ENC_ROWS && t < 2 * ENC_ROWS) ? tp : tb;
-            enc_comb_row(h, c, tab + (size_t)row * ENC_ENTRIES * 6);
+            if (half) enc_put<ACC>(c2, s2, i, h);
+            else enc_put<ACC>(c1, s1, i, h);
         }
-        enc_put<ACC>(c2, s2, i, h);
     }
 }
 
@@ -162,10 +176,12 @@ static cudaError_t encrypt_launch(View c1, View c2, size_t n, const uint8_t *r, 
     const size_t smem = 2 * ENC_TABLE_U4 * sizeof(uint4);
     cudaError_t e = ensure_smem_attr(g_enc_attr[ACC], (const void *)k_encrypt<ACC>, smem);
     if (e != cudaSuccess) return e;
-    const size_t need = (n + ENC_NT - 1) / ENC_NT, cap = (size_t)sm_count();
+    const int split = FT_ENC_SPLIT && c1.p != c2.p;
+    const size_t units = split ? 2 * n : n;
+    const size_t need = (units + ENC_NT - 1) / ENC_NT, cap = (size_t)sm_count();
     const unsigned grid = (unsigned)(need < cap ? need : cap);
     k_encrypt<ACC><<<grid, ENC_NT, smem, st>>>(c1.p, c1.s, c2.p, c2.s, n, (const uint4 *)r, m, mdig,
-                                               (const uint4 *)tables);
+                                               (const uint4 *)tables, split);
     return cudaGetLastError();
 }
 

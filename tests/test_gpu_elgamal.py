@@ -152,3 +152,38 @@ def test_encrypt_with_alternating_keys(ft, orc):
             o1, o2 = orc.encrypt(pks[j], m, r)
             assert (c1.to_bytes_folded() == orc.encode(o1)).all()
             assert (c2.to_bytes_folded() == orc.encode(o2)).all(), (rnd, j)
+
+
+@pytest.mark.parametrize("n", [1, 1000, 100001])
+def test_encrypt_and_rerandomise_halves(ft, orc, n):
+    """The encryption kernel computes c1 and c2 as separate work units (spread
+    over the grid) unless both are one array, in which case each thread does
+    c1's half, then c2's, as one call to each would: encrypting into one array
+    twice leaves c2's value, re-randomising it adds r*B then r*PK."""
+    torch = pytest.importorskip("torch")
+    g = synth.rng(140 + n)
+    sk, pk, pk_packed = keys(ft, g)
+    m = g.integers(0, 256, size=n, dtype=np.uint64)
+    r = synth.scalars_mod_L(g, n)
+    d_m = torch.from_numpy(m.view(np.int64)).cuda()
+    d_r = torch.from_numpy(r).cuda()
+    torch.cuda.synchronize()
+    rB = orc.from_scalars(r, threads=8)
+    rPK = orc.mul(np.repeat(pk_packed, n, axis=0), r, threads=8)
+    c2_want = orc.add(rPK, orc.from_scalars(orc.small_to_scalars(m), threads=8), threads=8)
+    # separate arrays: both halves as separate units
+    c1, c2 = ft.Array.init_scalar(n), ft.Array.init_scalar(n)
+    ft.encrypt_device(c1, c2, pk, d_m.data_ptr(), d_r.data_ptr(), n, 8)
+    assert (c1.to_bytes_folded() == orc.encode(rB, 8)).all()
+    assert (c2.to_bytes_folded() == orc.encode(c2_want, 8)).all()
+    # one array for both: c2's value wins, as with the halves in order
+    c = ft.Array.init_scalar(n)
+    ft.encrypt_device(c, c, pk, d_m.data_ptr(), d_r.data_ptr(), n, 8)
+    assert (c.to_bytes_folded() == orc.encode(c2_want, 8)).all()
+    # re-randomising one array as both halves adds r*B and r*PK
+    r2 = synth.scalars_mod_L(g, n)
+    before = c.to_packed()
+    ft.rerandomise(c, c, pk, r2)
+    want = orc.add(orc.add(before, orc.from_scalars(r2, threads=8), threads=8),
+                   orc.mul(np.repeat(pk_packed, n, axis=0), r2, threads=8), threads=8)
+    assert (c.to_bytes_folded() == orc.encode(want, 8)).all()
