@@ -28,6 +28,9 @@
 //            (replaces the reference's host std::sort, ftcrypto.cu:1170).
 #include <algorithm>
 
+#include <cmath>
+#include <mutex>
+
 #include "internal.h"
 #include "points.cuh"
 
@@ -164,6 +167,44 @@ struct ScanSet {
 #define FT_SEG_WALK_MINB 4
 #endif
 
+
+#ifndef FT_WAVE_FIT
+#define FT_WAVE_FIT 1
+#endif
+
+// Blocks of `fn` (block size `nt`, no dynamic shared memory) resident on the
+// whole GPU at once, from the occupancy calculator; cached by the caller.
+static int resident_blocks(const void *fn, int nt)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, nt, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return per_sm * sm_count();
+}
+
+// Of the points-per-thread candidates ks[0..nk) (ascending), the one whose
+// launch of ceil(ceil(n / k) / 128) * m blocks of 128 threads fills its last
+// wave of `resident` blocks best (waves / ceil(waves) highest; ties go to
+// the smaller k).  One walk per thread, so a last wave at 47% leaves half of
+// the GPU idle for 1/14 of the launch (2 x 4,194,304 points at 16 per
+// thread: 13.47 waves; at 18: 11.98).
+static int wave_fit_k(size_t n, int m, const int *ks, int nk, const int *resident)
+{
+    int best = ks[0];
+    double best_eff = -1.0;
+    for (int i = 0; i < nk; ++i) {
+        const size_t blocks = ((n + ks[i] - 1) / ks[i] + 127) / 128 * (size_t)m;
+        const double waves = (double)blocks / resident[i];
+        const double eff = waves / std::ceil(waves);
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = ks[i];
+        }
+    }
+    return best;
+}
 
 #ifndef FT_WALK_PAIRS
 #define FT_WALK_PAIRS 1
@@ -333,7 +374,21 @@ cudaError_t scan_set(const View *v, int m, size_t n, int exclusive, void *scratc
         k_scan_small<SMALL_NT><<<dim3(1, m), SMALL_NT, 0, st>>>(io, n, kpt, exclusive);
         return cudaGetLastError();
     }
-    const size_t K = scan_level_k(n);
+    // points per thread: 4 on the latency-bound lower levels; above 2^18
+    // points 16, 18 or 20, whichever fills the last wave best (at least
+    // 16, so the scratch sized for 16 suffices)
+    size_t K = scan_level_k(n);
+    if (FT_WAVE_FIT && K == 16) {
+        static const int ks[3] = {16, 18, 20};
+        static int res[3];
+        static std::once_flag once;
+        std::call_once(once, [] {
+            res[0] = resident_blocks((const void *)k_scan_sums<16>, 128);
+            res[1] = resident_blocks((const void *)k_scan_sums<18>, 128);
+            res[2] = resident_blocks((const void *)k_scan_sums<20>, 128);
+        });
+        K = (size_t)wave_fit_k(n, m, ks, 3, res);
+    }
     const size_t nt = (n + K - 1) / K;
     View ts[2];
     ScanSet tset{};
@@ -344,13 +399,21 @@ cudaError_t scan_set(const View *v, int m, size_t n, int exclusive, void *scratc
     }
     void *rest = (uint4 *)scratch + (size_t)m * FT_PLANES * nt;
     const dim3 grid((unsigned)((nt + 127) / 128), m);
-    if (K == 16) k_scan_sums<16><<<grid, 128, 0, st>>>(io, n, tset);
-    else k_scan_sums<4><<<grid, 128, 0, st>>>(io, n, tset);
+    switch (K) {
+    case 16: k_scan_sums<16><<<grid, 128, 0, st>>>(io, n, tset); break;
+    case 18: k_scan_sums<18><<<grid, 128, 0, st>>>(io, n, tset); break;
+    case 20: k_scan_sums<20><<<grid, 128, 0, st>>>(io, n, tset); break;
+    default: k_scan_sums<4><<<grid, 128, 0, st>>>(io, n, tset); break;
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if ((e = scan_set(ts, m, nt, 1, rest, st)) != cudaSuccess) return e;
-    if (K == 16) k_scan_apply<16><<<grid, 128, 0, st>>>(io, n, tset, exclusive);
-    else k_scan_apply<4><<<grid, 128, 0, st>>>(io, n, tset, exclusive);
+    switch (K) {
+    case 16: k_scan_apply<16><<<grid, 128, 0, st>>>(io, n, tset, exclusive); break;
+    case 18: k_scan_apply<18><<<grid, 128, 0, st>>>(io, n, tset, exclusive); break;
+    case 20: k_scan_apply<20><<<grid, 128, 0, st>>>(io, n, tset, exclusive); break;
+    default: k_scan_apply<4><<<grid, 128, 0, st>>>(io, n, tset, exclusive); break;
+    }
     return cudaGetLastError();
 }
 
@@ -535,14 +598,37 @@ cudaError_t segsum(View out, const int32_t *off, size_t nseg, View src, size_t n
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (nsrc == 0) return cudaSuccess;
-    const size_t nt = (nsrc + SEG_K - 1) / SEG_K;
+    // points per thread: 32, 36 or 40, whichever fills the walk's last wave
+    // best (at least 32, so the scratch sized for SEG_K suffices)
+    static const int ks[3] = {32, 36, 40};
+    static int res[3];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        res[0] = resident_blocks((const void *)k_seg_walk<32>, 128);
+        res[1] = resident_blocks((const void *)k_seg_walk<36>, 128);
+        res[2] = resident_blocks((const void *)k_seg_walk<40>, 128);
+    });
+    const int K = FT_WAVE_FIT ? wave_fit_k(nsrc, 1, ks, 3, res) : SEG_K;
+    const size_t nt = (nsrc + K - 1) / K;
     uint4 *H = (uint4 *)scratch;
     uint4 *Lp = H + FT_PLANES * nt;
     uint32_t *flags = (uint32_t *)(Lp + FT_PLANES * nt);
     int32_t *lseg = (int32_t *)(flags + nt);
     const unsigned grid = (unsigned)((nt + 127) / 128);
-    k_seg_walk<SEG_K><<<grid, 128, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s, (long long)nsrc, perm,
-                                             accumulate, H, Lp, nt, flags, lseg);
+    switch (K) {
+    case 36:
+        k_seg_walk<36><<<grid, 128, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s, (long long)nsrc, perm,
+                                              accumulate, H, Lp, nt, flags, lseg);
+        break;
+    case 40:
+        k_seg_walk<40><<<grid, 128, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s, (long long)nsrc, perm,
+                                              accumulate, H, Lp, nt, flags, lseg);
+        break;
+    default:
+        k_seg_walk<SEG_K><<<grid, 128, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s, (long long)nsrc, perm,
+                                                 accumulate, H, Lp, nt, flags, lseg);
+        break;
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_seg_join<<<grid, 128, 0, st>>>(out.p, out.s, H, Lp, nt, flags, lseg, nt, accumulate);
     return cudaGetLastError();
