@@ -187,9 +187,9 @@ static int resident_blocks(const void *fn, int nt)
 // Of the points-per-thread candidates ks[0..nk) (ascending), the one whose
 // launch of ceil(ceil(n / k) / 128) * m blocks of 128 threads fills its last
 // wave of `resident` blocks best (waves / ceil(waves) highest; ties go to
-// the smaller k).  One walk per thread, so a last wave at 47% leaves half of
-// the GPU idle for 1/14 of the launch (2 x 4,194,304 points at 16 per
-// thread: 13.47 waves; at 18: 11.98).
+// the smaller k).  One walk per thread, so a last wave at 74% leaves a
+// quarter of the GPU idle for 1/7 of the launch (16,777,216 points at 32 per
+// thread in four 128-thread blocks per SM: 6.74 waves; at 36: 5.99).
 static int wave_fit_k(size_t n, int m, const int *ks, int nk, const int *resident)
 {
     int best = ks[0];
@@ -374,21 +374,11 @@ cudaError_t scan_set(const View *v, int m, size_t n, int exclusive, void *scratc
         k_scan_small<SMALL_NT><<<dim3(1, m), SMALL_NT, 0, st>>>(io, n, kpt, exclusive);
         return cudaGetLastError();
     }
-    // points per thread: 4 on the latency-bound lower levels; above 2^18
-    // points 16, 18 or 20, whichever fills the last wave best (at least
-    // 16, so the scratch sized for 16 suffices)
-    size_t K = scan_level_k(n);
-    if (FT_WAVE_FIT && K == 16) {
-        static const int ks[3] = {16, 18, 20};
-        static int res[3];
-        static std::once_flag once;
-        std::call_once(once, [] {
-            res[0] = resident_blocks((const void *)k_scan_sums<16>, 128);
-            res[1] = resident_blocks((const void *)k_scan_sums<18>, 128);
-            res[2] = resident_blocks((const void *)k_scan_sums<20>, 128);
-        });
-        K = (size_t)wave_fit_k(n, m, ks, 3, res);
-    }
+    // points per thread: 16 above 2^18 points, 4 on the latency-bound lower
+    // levels.  (Choosing 16, 18 or 20 by how well the last wave fills, as
+    // the segmented walk does, measured 7% slower: at 18 and 20 points the
+    // sums pass takes 170 registers and two blocks per SM instead of three.)
+    const size_t K = scan_level_k(n);
     const size_t nt = (n + K - 1) / K;
     View ts[2];
     ScanSet tset{};
@@ -399,21 +389,13 @@ cudaError_t scan_set(const View *v, int m, size_t n, int exclusive, void *scratc
     }
     void *rest = (uint4 *)scratch + (size_t)m * FT_PLANES * nt;
     const dim3 grid((unsigned)((nt + 127) / 128), m);
-    switch (K) {
-    case 16: k_scan_sums<16><<<grid, 128, 0, st>>>(io, n, tset); break;
-    case 18: k_scan_sums<18><<<grid, 128, 0, st>>>(io, n, tset); break;
-    case 20: k_scan_sums<20><<<grid, 128, 0, st>>>(io, n, tset); break;
-    default: k_scan_sums<4><<<grid, 128, 0, st>>>(io, n, tset); break;
-    }
+    if (K == 16) k_scan_sums<16><<<grid, 128, 0, st>>>(io, n, tset);
+    else k_scan_sums<4><<<grid, 128, 0, st>>>(io, n, tset);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if ((e = scan_set(ts, m, nt, 1, rest, st)) != cudaSuccess) return e;
-    switch (K) {
-    case 16: k_scan_apply<16><<<grid, 128, 0, st>>>(io, n, tset, exclusive); break;
-    case 18: k_scan_apply<18><<<grid, 128, 0, st>>>(io, n, tset, exclusive); break;
-    case 20: k_scan_apply<20><<<grid, 128, 0, st>>>(io, n, tset, exclusive); break;
-    default: k_scan_apply<4><<<grid, 128, 0, st>>>(io, n, tset, exclusive); break;
-    }
+    if (K == 16) k_scan_apply<16><<<grid, 128, 0, st>>>(io, n, tset, exclusive);
+    else k_scan_apply<4><<<grid, 128, 0, st>>>(io, n, tset, exclusive);
     return cudaGetLastError();
 }
 
