@@ -212,6 +212,9 @@ static int wave_fit_k(size_t n, int m, const int *ks, int nk, const int *residen
 #ifndef FT_SCAN_PREFETCH
 #define FT_SCAN_PREFETCH 0
 #endif
+#ifndef FT_SEG_PREFETCH
+#define FT_SEG_PREFETCH 0
+#endif
 
 // per-thread sums of K consecutive points: ts[t] = sum of p[tK .. tK+K).
 // With FT_WALK_PAIRS the thread loads its points two at a time: the two
@@ -497,6 +500,18 @@ __global__ void __launch_bounds__(128, FT_SEG_WALK_MINB) k_seg_walk(uint4 *op, s
         int sg = live ? upper_bound_i32(off, 0, nseg + 1, e0) - 1 : 0; // segment holding e0 (skips empty ones)
         bool open_before = live && (long long)off[sg] < e0;
         uint32_t fl = 0;
+#if FT_SEG_PREFETCH
+        // the thread's K points (every 128-byte line of each plane) towards
+        // L2 before the walk (not for a gather through perm)
+        if (live && !perm) {
+#pragma unroll
+            for (int k = 0; k < FT_PLANES; ++k) {
+#pragma unroll
+                for (int q = 0; q < K; q += 8)
+                    if (e0 + q < e1) asm volatile("prefetch.global.L2 [%0];" ::"l"(sp + k * ss + (size_t)(e0 + q)));
+            }
+        }
+#endif
         ge_p3 acc;
         ge_p3_0(acc);
         // every thread of the block takes the K steps, with a barrier each:
