@@ -209,12 +209,6 @@ static int wave_fit_k(size_t n, int m, const int *ks, int nk, const int *residen
 #ifndef FT_WALK_PAIRS
 #define FT_WALK_PAIRS 1
 #endif
-#ifndef FT_SCAN_PREFETCH
-#define FT_SCAN_PREFETCH 0
-#endif
-#ifndef FT_SEG_PREFETCH
-#define FT_SEG_PREFETCH 0
-#endif
 
 // per-thread sums of K consecutive points: ts[t] = sum of p[tK .. tK+K).
 // With FT_WALK_PAIRS the thread loads its points two at a time: the two
@@ -282,19 +276,6 @@ __global__ void __launch_bounds__(128, FT_SCAN_APPLY_MINB) k_scan_apply(ScanSet 
     const size_t nt = (n + K - 1) / K;
     FT_GRID_LOOP(t, nt)
     {
-#if FT_SCAN_PREFETCH
-        // bring the thread's K points (every 128-byte line of each plane)
-        // towards L2 before the walk, so the loads of later pairs, which wait
-        // behind the stores of earlier ones, find them there
-#pragma unroll
-        for (int k = 0; k < FT_PLANES; ++k) {
-#pragma unroll
-            for (int q = 0; q < K; q += 8) {
-                const size_t e = t * K + q;
-                if (e < n) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + k * s + e));
-            }
-        }
-#endif
         ge_p3 pre;
         ld_p3(pre, tp, tss, t);
 #if FT_WALK_PAIRS
@@ -500,18 +481,6 @@ __global__ void __launch_bounds__(128, FT_SEG_WALK_MINB) k_seg_walk(uint4 *op, s
         int sg = live ? upper_bound_i32(off, 0, nseg + 1, e0) - 1 : 0; // segment holding e0 (skips empty ones)
         bool open_before = live && (long long)off[sg] < e0;
         uint32_t fl = 0;
-#if FT_SEG_PREFETCH
-        // the thread's K points (every 128-byte line of each plane) towards
-        // L2 before the walk (not for a gather through perm)
-        if (live && !perm) {
-#pragma unroll
-            for (int k = 0; k < FT_PLANES; ++k) {
-#pragma unroll
-                for (int q = 0; q < K; q += 8)
-                    if (e0 + q < e1) asm volatile("prefetch.global.L2 [%0];" ::"l"(sp + k * ss + (size_t)(e0 + q)));
-            }
-        }
-#endif
         ge_p3 acc;
         ge_p3_0(acc);
         // every thread of the block takes the K steps, with a barrier each:
