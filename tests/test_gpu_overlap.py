@@ -170,3 +170,35 @@ def test_server_write_after_mark_is_seen(ft, orc):
         assert (c2.to_bytes_folded() == orc.encode(orc.mul(orc.mul(p2, k1, threads=8), k2, threads=8), 8)).all()
     finally:
         srv.close()
+
+
+def test_length_changes_after_mark(ft, orc):
+    """A marked array shortened in place (to more than half its length: same
+    storage) exports its first n points on the overlapped path; lengthened
+    (the new points set to the identity, a use of the storage) or shortened
+    to half or less (new storage) it exports in stream order."""
+    torch = pytest.importorskip("torch")
+    g = synth.rng(77)
+    n = 3001
+    p = orc.from_scalars(synth.scalars_mod_L(g, n), threads=8)
+    k = synth.scalars_mod_L(g, n)
+    want = orc.encode(orc.mul(p, k, threads=8), 8)
+    ident = ft.Array.init_scalar(1).to_bytes_folded()[0]
+    c = ft.Array.from_packed(p)
+    c.mul(pinned(torch, k))
+    c.set_length(2000)
+    assert (c.to_bytes_folded() == want[:2000]).all()
+    c.set_length(2600)
+    got = c.to_bytes_folded()
+    assert (got[:2000] == want[:2000]).all() and (got[2000:] == ident).all()
+    c.set_length(6000)
+    got = c.to_bytes_folded()
+    assert (got[:2000] == want[:2000]).all() and (got[2000:] == ident).all()
+    c.mul(pinned(torch, np.tile(k[:1], (6000, 1))))
+    c.set_length(1000)
+    assert (c.to_bytes_folded() == orc.encode(orc.mul(orc.mul(p[:1000], k[:1000], threads=8),
+                                                      np.tile(k[:1], (1000, 1)), threads=8), 8)).all()
+    # one point, pinned scalars, export right away
+    one = ft.Array.from_packed(p[:1])
+    one.mul(pinned(torch, k[:1]))
+    assert (raw(ft, one, torch) == orc.to_ref160(orc.mul(p[:1], k[:1]))).all()
