@@ -63,7 +63,7 @@ struct SmemTab {
 
 // Entries 0-3 in shared memory ([entry][word][thread], stride NT), entries
 // 4-7 in TMEM at columns col + 32 j + 8 (k - 4) of the thread's lane: the
-// four entries' coordinate j are 32 consecutive columns, read by one load.
+// four entries' coordinate j are 32 consecutive columns (read 8 at a time).
 template <int NT>
 struct HybridTab {
     uint4 *b;     // &smem[threadIdx.x]
