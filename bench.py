@@ -459,8 +459,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     d_off = torch.from_numpy(off).cuda()
     torch.cuda.synchronize()
     o1, o2 = ft.Array.init_scalar(nseg), ft.Array.init_scalar(nseg)
-    ft.segmented_sum_csr_device(o1, d_off.data_ptr(), nseg, c1)
-    ft.segmented_sum_csr_device(o2, d_off.data_ptr(), nseg, c2)
+    ft.ct_segmented_sum_csr_device(o1, o2, d_off.data_ptr(), nseg, c1, c2)
     segm = np.add.reduceat(m3, off[:-1]).astype(np.uint64)
     ok_seg = decrypt_matches(ft, o1, o2, sk[0], segm)
     red_pairs, seg_pairs = [], []
@@ -472,8 +471,7 @@ def extras(ft, synth, torch, st, hbm_peak, imad):
     ms = timed(ev, lambda: (c1.reduce_into(r1, 0), c2.reduce_into(r2, 0)), 11)
     out["reduce_16M_ct"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok, **oracle_check(red_pairs),
                             **roof(2 * n3 * B_PT, 2 * n3 * W_ALG_PTADD, ms, hbm_peak, imad)}
-    ms = timed(ev, lambda: (ft.segmented_sum_csr_device(o1, d_off.data_ptr(), nseg, c1),
-                            ft.segmented_sum_csr_device(o2, d_off.data_ptr(), nseg, c2)), 11)
+    ms = timed(ev, lambda: ft.ct_segmented_sum_csr_device(o1, o2, d_off.data_ptr(), nseg, c1, c2), 11)
     seg_bytes = 2 * (n3 * B_PT + nseg * B_PT) + (nseg + 1) * 4
     out["segsum_16M_ct_1M_seg"] = {"ct_per_s": n3 / (ms * 1e-3), "ms": ms, "decrypt_check": ok_seg,
                                    **oracle_check(seg_pairs),

@@ -105,6 +105,16 @@ ft_error ftx_segmented_sum_csr(ft_ge25519_array *out, const int32_t *offsets, si
 ft_error ftx_segmented_sum_csr_device(ft_ge25519_array out, const int32_t *d_offsets, size_t nseg,
                                       const_ft_ge25519_array src);
 
+/* Ciphertext segmented sum: ftx_segmented_sum_csr_device of c1 into out1 and
+ * of c2 into out2 over the same device offsets, both halves through the
+ * same launches (the segmented sum of ft_reduce_isum, ftcrypto.cu:1113-1217,
+ * over the CSR layout, applied to each half of a ciphertext array).  c1 and
+ * c2 of one length, out1 and out2 of length nseg; where an output is the
+ * other half's input or output the two sums run in order, as two calls
+ * would (the second then reads what the first wrote). */
+ft_error ftx_ct_segmented_sum_csr_device(ft_ge25519_array out1, ft_ge25519_array out2, const int32_t *d_offsets,
+                                         size_t nseg, const_ft_ge25519_array c1, const_ft_ge25519_array c2);
+
 /* out[out_idx] = sum of src, leaving src unchanged. */
 ft_error ftx_reduce_into(ft_ge25519_array out, size_t out_idx, const_ft_ge25519_array src);
 

@@ -12,7 +12,7 @@ The C library is the product; this package builds it (build.py), binds it
 """
 from .api import (AFFINE, DECRYPT_MAX_M, EXTENDED, FOLDED, NO_PLAINTEXT, PACKED, TUNE_BATCH_ADD_PTS,  # noqa: F401
                   TUNE_LADDER_BLOCK, TUNE_SCALE_WINDOW, Array, Batch, FtError, check, decrypt, device_memory, encrypt, encrypt_device,
-                  ct_add, ct_scan, ct_sub, error_str, init, rerandomise, rerandomise_device, Server, segmented_sum_csr,
+                  ct_add, ct_scan, ct_segmented_sum_csr_device, ct_sub, error_str, init, rerandomise, rerandomise_device, Server, segmented_sum_csr,
                   segmented_sum_csr_device, stream_handle, synchronize, tune, tune_get)
 from .build import LIB as LIB_PATH  # noqa: F401
 from .build import build  # noqa: F401

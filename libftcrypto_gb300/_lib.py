@@ -79,6 +79,7 @@ SIGNATURES = {
     "ftx_decrypt": (I, [P, P, P, ctypes.c_uint64, P]),
     "ftx_segmented_sum_csr": (I, [PP, P, S, P]),
     "ftx_segmented_sum_csr_device": (I, [P, P, S, P]),
+    "ftx_ct_segmented_sum_csr_device": (I, [P, P, P, S, P, P]),
     "ftx_reduce_into": (I, [P, S, P]),
     "ftx_scale_small": (I, [P, ctypes.c_uint32]),
     "ftx_scale_bounded": (I, [P, ctypes.c_uint32, U]),

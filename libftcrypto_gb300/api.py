@@ -346,6 +346,13 @@ def segmented_sum_csr_device(out: Array, d_offsets: int, nseg: int, src: Array) 
     check(lib().ftx_segmented_sum_csr_device(out.handle, ctypes.c_void_p(d_offsets), nseg, src.handle))
 
 
+def ct_segmented_sum_csr_device(out1: Array, out2: Array, d_offsets: int, nseg: int, c1: Array, c2: Array) -> None:
+    """ftx_ct_segmented_sum_csr_device: both halves of a ciphertext array over
+    the same device offsets in the same launches."""
+    check(lib().ftx_ct_segmented_sum_csr_device(out1.handle, out2.handle, ctypes.c_void_p(d_offsets), nseg,
+                                                c1.handle, c2.handle))
+
+
 class Batch:
     """ftx_batch: many independent array operations in one persistent launch
     replayed from a CUDA graph.  Keeps references to its arrays."""

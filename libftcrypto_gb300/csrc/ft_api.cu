@@ -1291,6 +1291,26 @@ ft_error ftx_segmented_sum_csr_device(ft_ge25519_array out, const int32_t *d_off
     return FT_ERR_NO_ERROR;
 }
 
+ft_error ftx_ct_segmented_sum_csr_device(ft_ge25519_array out1, ft_ge25519_array out2, const int32_t *d_off,
+                                         size_t nseg, const_ft_ge25519_array src1, const_ft_ge25519_array src2)
+{
+    ENSURE_INIT();
+    if (out1->n != nseg || out2->n != nseg || src1->n != src2->n) return FT_ERR_SIZE_MISMATCH;
+    if (src1->n >= (size_t)INT32_MAX || nseg >= (size_t)INT32_MAX) return FT_ERR_BAD_SIZE;
+    if (out1 == out2 || out1 == src2 || out2 == src1) {
+        // one half's output is the other's input or output: the two sums
+        // in order, as the two calls they stand for
+        ft_error err = ftx_segmented_sum_csr_device(out1, d_off, nseg, src1);
+        return err ? err : ftx_segmented_sum_csr_device(out2, d_off, nseg, src2);
+    }
+    void *s;
+    CK(scratch(&s, ft::segsum_scratch_bytes(src1->n, 2)));
+    const View outs[2] = {ft::view_of(out1), ft::view_of(out2)};
+    const View srcs[2] = {ft::view_of(src1), ft::view_of(src2)};
+    CK(ft::segsum_set(outs, srcs, 2, d_off, nseg, src1->n, nullptr, 0, s, g.stream));
+    return FT_ERR_NO_ERROR;
+}
+
 ft_error ftx_segmented_sum_csr(ft_ge25519_array *out, const int32_t *off, size_t nseg, const_ft_ge25519_array src)
 {
     ENSURE_INIT();

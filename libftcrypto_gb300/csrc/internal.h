@@ -150,9 +150,13 @@ cudaError_t scan(View v, size_t n, int exclusive, void *d_scratch, cudaStream_t 
 // m (1 or 2) arrays of n points each scanned by the same launches
 cudaError_t scan_set(const View *v, int m, size_t n, int exclusive, void *d_scratch, cudaStream_t st);
 // out[s] (+)= sum of src[perm ? perm[e] : e] for e in [off[s], off[s+1])
-size_t segsum_scratch_bytes(size_t nsrc);
+size_t segsum_scratch_bytes(size_t nsrc, int m = 1);
 cudaError_t segsum(View out, const int32_t *d_off, size_t nseg, View src, size_t nsrc,
                    const int32_t *d_perm, int accumulate, void *d_scratch, cudaStream_t st);
+// m (1 or 2) segmented sums over the same offsets (out[i] from src[i]) by the
+// same launches; scratch of segsum_scratch_bytes(nsrc, m)
+cudaError_t segsum_set(const View *out, const View *src, int m, const int32_t *d_off, size_t nseg, size_t nsrc,
+                       const int32_t *d_perm, int accumulate, void *d_scratch, cudaStream_t st);
 // the same sums as segsum through one inclusive scan of the (gathered) points
 // and a difference of two prefixes per segment: for layouts with long
 // segments, which the walk's join adds up one thread part after another

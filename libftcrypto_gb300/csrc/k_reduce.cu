@@ -462,16 +462,41 @@ FT_DEV void seg_write(uint4 *op, size_t os, int sg, const ge_p3 &v, int accumula
 #define SEG_CLOSE 2u  // ... and that segment ends inside the thread (or at its last point)
 #define SEG_TAIL 4u   // L[t] holds the start of segment lseg[t], which continues past the thread
 
+// The arrays of one or two segmented sums over the same offsets (the two
+// halves of a ciphertext array): output, source and scratch of sum y in
+// slot y, chosen by blockIdx.y (a select, not an index, so the struct stays
+// in parameter space).
+struct SegSet {
+    uint4 *op[2];
+    size_t os[2];
+    const uint4 *sp[2];
+    size_t ss[2];
+    uint4 *H[2];
+    uint4 *Lp[2];
+    uint32_t *flags[2];
+    int32_t *lseg[2];
+    template <class T>
+    FT_DEV static T pick(const T (&a)[2]) { return blockIdx.y ? a[1] : a[0]; }
+};
+
 // Pass 1: thread t sums its K consecutive points segment by segment.  A
 // segment that begins and ends inside the thread is written at once; the
 // parts of segments crossing the thread's edges go to H / L.
 // four blocks per SM (128 registers, a few spills to L1) rather than two at
 // 202 registers: 2.58 against 2.68 ms for 16,777,216 points (measured)
 template <int K>
-__global__ void __launch_bounds__(128, FT_SEG_WALK_MINB) k_seg_walk(uint4 *op, size_t os, const int32_t *off, int nseg, const uint4 *sp,
-                                                  size_t ss, long long nsrc, const int32_t *perm, int accumulate,
-                                                  uint4 *H, uint4 *Lp, size_t hs, uint32_t *flags, int32_t *lseg)
+__global__ void __launch_bounds__(128, FT_SEG_WALK_MINB) k_seg_walk(SegSet set, const int32_t *off, int nseg,
+                                                                    long long nsrc, const int32_t *perm, int accumulate,
+                                                                    size_t hs)
 {
+    uint4 *op = SegSet::pick(set.op);
+    const size_t os = SegSet::pick(set.os);
+    const uint4 *sp = SegSet::pick(set.sp);
+    const size_t ss = SegSet::pick(set.ss);
+    uint4 *H = SegSet::pick(set.H);
+    uint4 *Lp = SegSet::pick(set.Lp);
+    uint32_t *flags = SegSet::pick(set.flags);
+    int32_t *lseg = SegSet::pick(set.lseg);
     const long long nt = (nsrc + K - 1) / K;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; // the launch covers nt
     const bool live = t < nt;
@@ -523,9 +548,14 @@ __global__ void __launch_bounds__(128, FT_SEG_WALK_MINB) k_seg_walk(uint4 *op, s
 
 // Pass 2: a segment started in thread t and continuing past it totals
 // L[t] + H[t+1] + ... + H[u], u the first later thread whose head closes it.
-__global__ void __launch_bounds__(128) k_seg_join(uint4 *op, size_t os, const uint4 *H, const uint4 *Lp, size_t hs,
-                                                  const uint32_t *flags, const int32_t *lseg, size_t nt, int accumulate)
+__global__ void __launch_bounds__(128) k_seg_join(SegSet set, size_t hs, size_t nt, int accumulate)
 {
+    uint4 *op = SegSet::pick(set.op);
+    const size_t os = SegSet::pick(set.os);
+    const uint4 *H = SegSet::pick(set.H);
+    const uint4 *Lp = SegSet::pick(set.Lp);
+    const uint32_t *flags = SegSet::pick(set.flags);
+    const int32_t *lseg = SegSet::pick(set.lseg);
     FT_GRID_LOOP(t, nt)
     {
         if (!(flags[t] & SEG_TAIL)) continue;
@@ -542,8 +572,10 @@ __global__ void __launch_bounds__(128) k_seg_join(uint4 *op, size_t os, const ui
     }
 }
 
-__global__ void __launch_bounds__(256) k_seg_empty(uint4 *op, size_t os, const int32_t *off, size_t nseg)
+__global__ void __launch_bounds__(256) k_seg_empty(SegSet set, const int32_t *off, size_t nseg)
 {
+    uint4 *op = SegSet::pick(set.op);
+    const size_t os = SegSet::pick(set.os);
     FT_GRID_LOOP(sg, nseg)
     {
         if (off[sg] == off[sg + 1]) {
@@ -560,23 +592,35 @@ __global__ void __launch_bounds__(256) k_seg_empty(uint4 *op, size_t os, const i
 // 128 measure the same as 32; 8 is 3.84 ms)
 static const int SEG_K = 32;
 
-size_t segsum_scratch_bytes(size_t nsrc)
+size_t segsum_scratch_bytes(size_t nsrc, int m)
 {
     size_t nt = (nsrc + SEG_K - 1) / SEG_K;
-    return 2 * nt * 128 + 2 * nt * 4 + 1024;
+    const size_t one = ((2 * nt * 128 + 2 * nt * 4 + 1024) + 255) / 256 * 256; // each sum's part 256-byte aligned
+    return (size_t)m * one;
 }
 
 // out[s] (+)= sum of src[perm ? perm[e] : e], e in [off[s], off[s+1]):
 // ~1 + 1/SEG_K additions per point, two kernels, no waits between blocks.
 // A segment spanning m threads costs m sequential additions in pass 2
-// (m ~ length / 32; 1-2 for the benchmark's mean lengths 8-32).
-cudaError_t segsum(View out, const int32_t *off, size_t nseg, View src, size_t nsrc, const int32_t *perm,
-                   int accumulate, void *scratch, cudaStream_t st)
+// (m ~ length / 32; 1-2 for the benchmark's mean lengths 8-32).  m (1 or
+// 2) sums over the same offsets and source length go through the same
+// launches (grid dimension y); scratch holds m x segsum_scratch_bytes(nsrc).
+cudaError_t segsum_set(const View *out, const View *src, int m, const int32_t *off, size_t nseg, size_t nsrc,
+                       const int32_t *perm, int accumulate, void *scratch, cudaStream_t st)
 {
     if (nseg == 0) return cudaSuccess;
+    if (m < 1 || m > 2) return cudaErrorInvalidValue;
+    SegSet set{};
+    for (int i = 0; i < m; ++i) {
+        set.op[i] = out[i].p;
+        set.os[i] = out[i].s;
+        set.sp[i] = src[i].p;
+        set.ss[i] = src[i].s;
+    }
     cudaError_t e;
     if (!accumulate) {
-        k_seg_empty<<<(unsigned)std::min<size_t>((nseg + 255) / 256, 65535), 256, 0, st>>>(out.p, out.s, off, nseg);
+        const dim3 g((unsigned)std::min<size_t>((nseg + 255) / 256, 65535), m);
+        k_seg_empty<<<g, 256, 0, st>>>(set, off, nseg);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (nsrc == 0) return cudaSuccess;
@@ -590,30 +634,30 @@ cudaError_t segsum(View out, const int32_t *off, size_t nseg, View src, size_t n
         res[1] = resident_blocks((const void *)k_seg_walk<36>, 128);
         res[2] = resident_blocks((const void *)k_seg_walk<40>, 128);
     });
-    const int K = FT_WAVE_FIT ? wave_fit_k(nsrc, 1, ks, 3, res) : SEG_K;
+    const int K = FT_WAVE_FIT ? wave_fit_k(nsrc, m, ks, 3, res) : SEG_K;
     const size_t nt = (nsrc + K - 1) / K;
-    uint4 *H = (uint4 *)scratch;
-    uint4 *Lp = H + FT_PLANES * nt;
-    uint32_t *flags = (uint32_t *)(Lp + FT_PLANES * nt);
-    int32_t *lseg = (int32_t *)(flags + nt);
-    const unsigned grid = (unsigned)((nt + 127) / 128);
+    for (int i = 0; i < m; ++i) {
+        uint8_t *base = (uint8_t *)scratch + (size_t)i * segsum_scratch_bytes(nsrc, 1);
+        set.H[i] = (uint4 *)base;
+        set.Lp[i] = set.H[i] + FT_PLANES * nt;
+        set.flags[i] = (uint32_t *)(set.Lp[i] + FT_PLANES * nt);
+        set.lseg[i] = (int32_t *)(set.flags[i] + nt);
+    }
+    const dim3 grid((unsigned)((nt + 127) / 128), m);
     switch (K) {
-    case 36:
-        k_seg_walk<36><<<grid, 128, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s, (long long)nsrc, perm,
-                                              accumulate, H, Lp, nt, flags, lseg);
-        break;
-    case 40:
-        k_seg_walk<40><<<grid, 128, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s, (long long)nsrc, perm,
-                                              accumulate, H, Lp, nt, flags, lseg);
-        break;
-    default:
-        k_seg_walk<SEG_K><<<grid, 128, 0, st>>>(out.p, out.s, off, (int)nseg, src.p, src.s, (long long)nsrc, perm,
-                                                 accumulate, H, Lp, nt, flags, lseg);
-        break;
+    case 36: k_seg_walk<36><<<grid, 128, 0, st>>>(set, off, (int)nseg, (long long)nsrc, perm, accumulate, nt); break;
+    case 40: k_seg_walk<40><<<grid, 128, 0, st>>>(set, off, (int)nseg, (long long)nsrc, perm, accumulate, nt); break;
+    default: k_seg_walk<SEG_K><<<grid, 128, 0, st>>>(set, off, (int)nseg, (long long)nsrc, perm, accumulate, nt); break;
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_seg_join<<<grid, 128, 0, st>>>(out.p, out.s, H, Lp, nt, flags, lseg, nt, accumulate);
+    k_seg_join<<<grid, 128, 0, st>>>(set, nt, nt, accumulate);
     return cudaGetLastError();
+}
+
+cudaError_t segsum(View out, const int32_t *off, size_t nseg, View src, size_t nsrc, const int32_t *perm,
+                   int accumulate, void *scratch, cudaStream_t st)
+{
+    return segsum_set(&out, &src, 1, off, nseg, nsrc, perm, accumulate, scratch, st);
 }
 
 // ------------------------------------------------------------ long segments

@@ -223,19 +223,25 @@ ft_error ftx_server_s::dispatch(Req *q, Slot &sl)
         break;
     }
     case FTX_REQ_SEGSUM: {
-        void *doff, *s1, *s2;
+        void *doff, *s;
         e = new_array(&q->res.c1, r.nseg, st);
         if (e == cudaSuccess) e = new_array(&q->res.c2, r.nseg, st);
         if (e == cudaSuccess) e = alloc_on(q, &doff, (r.nseg + 1) * 4, st);
         const size_t sb = q->seg_prefix ? ft::segsum_prefix_scratch_bytes(r.n) : ft::segsum_scratch_bytes(r.n);
-        auto sum = q->seg_prefix ? ft::segsum_prefix : ft::segsum;
-        if (e == cudaSuccess) e = alloc_on(q, &s1, sb, st);
-        if (e == cudaSuccess) e = alloc_on(q, &s2, sb, st);
+        if (e == cudaSuccess) e = alloc_on(q, &s, 2 * sb, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(doff, r.offsets, (r.nseg + 1) * 4, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess)
-            e = sum(ft::view_of(q->res.c1), (const int32_t *)doff, r.nseg, ft::view_of(r.c1), r.n, nullptr, 0, s1, st);
-        if (e == cudaSuccess)
-            e = sum(ft::view_of(q->res.c2), (const int32_t *)doff, r.nseg, ft::view_of(r.c2), r.n, nullptr, 0, s2, st);
+        if (e == cudaSuccess && q->seg_prefix) {
+            e = ft::segsum_prefix(ft::view_of(q->res.c1), (const int32_t *)doff, r.nseg, ft::view_of(r.c1), r.n,
+                                  nullptr, 0, s, st);
+            if (e == cudaSuccess)
+                e = ft::segsum_prefix(ft::view_of(q->res.c2), (const int32_t *)doff, r.nseg, ft::view_of(r.c2), r.n,
+                                      nullptr, 0, (uint8_t *)s + sb, st);
+        } else if (e == cudaSuccess) {
+            // both halves through the same walk and join launches
+            const ft::View outs[2] = {ft::view_of(q->res.c1), ft::view_of(q->res.c2)};
+            const ft::View srcs[2] = {ft::view_of(r.c1), ft::view_of(r.c2)};
+            e = ft::segsum_set(outs, srcs, 2, (const int32_t *)doff, r.nseg, r.n, nullptr, 0, s, st);
+        }
         break;
     }
     default: return FT_ERR_BAD_SIZE;

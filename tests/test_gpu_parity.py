@@ -484,6 +484,39 @@ def test_segmented_sum_long_segments_both_paths(ft, orc):
     assert (out.to_bytes_folded() == want).all()
 
 
+@pytest.mark.parametrize("n,nseg", [(1, 1), (1000, 63), (70000, 2000), (300001, 20000)])
+def test_ct_segmented_sum_both_halves(ft, orc, n, nseg):
+    """Both halves of a ciphertext array summed over the same device offsets
+    in one set of launches equal the oracle's segment sums of each half, with
+    empty segments in the layout; outputs that alias the other half's input
+    take the two single-array calls in order."""
+    torch = pytest.importorskip("torch")
+    g = synth.rng(700 + n)
+    a1, a2 = rand_points(orc, g, n), rand_points(orc, g, n)
+    off = synth.csr_offsets(g, n, nseg)
+    if nseg > 2:
+        off[1] = off[0]  # an empty first segment
+        off[-2] = off[-1]  # and an empty last one
+    w1 = orc.encode(orc.segsum_csr(off, a1, threads=8))
+    w2 = orc.encode(orc.segsum_csr(off, a2, threads=8))
+    d_off = torch.from_numpy(off).cuda()
+    torch.cuda.synchronize()
+    C1, C2 = upload(ft, a1), upload(ft, a2)
+    o1, o2 = ft.Array.init_scalar(nseg), ft.Array.init_scalar(nseg)
+    ft.ct_segmented_sum_csr_device(o1, o2, d_off.data_ptr(), nseg, C1, C2)
+    assert (o1.to_bytes_folded() == w1).all()
+    assert (o2.to_bytes_folded() == w2).all()
+    if n == nseg:
+        # one point a segment, out1 = c2: the two sums in order, the second
+        # reading the first's result (each sum the identity map here)
+        ft.ct_segmented_sum_csr_device(C2, o2, d_off.data_ptr(), nseg, C1, C2)
+        assert (C2.to_bytes_folded() == w1).all()
+        assert (o2.to_bytes_folded() == w1).all()
+    with pytest.raises(ft.FtError) as e:
+        ft.ct_segmented_sum_csr_device(o1, ft.Array.init_scalar(nseg + 1), d_off.data_ptr(), nseg, C1, C2)
+    assert e.value.code == 2
+
+
 @pytest.mark.parametrize("n", [1, 2, 1000, 1 << 20])
 def test_reduce_isum_all_keys_equal(ft, orc, n):
     """Every key the same (one segment of n points, a full reduction) and
