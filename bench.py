@@ -956,9 +956,8 @@ def run_ours(args):
     return 0
 
 
-PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan", "ct_scan", "segsum", "isum",
-                 "isum_one_key", "encode",
-                 "decode", "batch", "export", "int_peaks")
+PROFILE_CASES = ("ladder", "encrypt", "comb", "add", "ct_add", "reduce", "scan", "ct_scan", "segsum", "ct_segsum",
+                 "isum", "isum_one_key", "encode", "decode", "batch", "export", "int_peaks")
 
 
 def run_profile(case: str, size: int | None = None) -> int:
@@ -998,8 +997,8 @@ def run_profile(case: str, size: int | None = None) -> int:
         op = lambda: ft.encrypt_device(c1, c2, pk, m.data_ptr(), d_sc.data_ptr(), n, 8)  # noqa: E731
     elif case == "comb":
         op = lambda: ft.Array.from_scalars(sc)  # noqa: E731
-    elif case in ("add", "reduce", "scan", "ct_scan", "segsum", "isum", "isum_one_key"):
-        big = size or (1 << 24 if case in ("reduce", "segsum") else 1 << 22)
+    elif case in ("add", "reduce", "scan", "ct_scan", "segsum", "ct_segsum", "isum", "isum_one_key"):
+        big = size or (1 << 24 if case in ("reduce", "segsum", "ct_segsum") else 1 << 22)
         a = ft.Array.init_point(big, base, 3)
         a.add(ft.Array.init_point(big, base, 5))
         if case == "add":
@@ -1019,6 +1018,13 @@ def run_profile(case: str, size: int | None = None) -> int:
             torch.cuda.synchronize()
             out = ft.Array.init_scalar(big // 16)
             op = lambda: ft.segmented_sum_csr_device(out, d_off.data_ptr(), big // 16, a)  # noqa: E731
+        elif case == "ct_segsum":  # both halves of `big` ciphertexts over the same offsets
+            a2 = ft.Array.init_point(big, base, 7)
+            off = synth.csr_offsets(g, big, big // 16)
+            d_off = torch.from_numpy(off).cuda()
+            torch.cuda.synchronize()
+            o1, o2 = ft.Array.init_scalar(big // 16), ft.Array.init_scalar(big // 16)
+            op = lambda: ft.ct_segmented_sum_csr_device(o1, o2, d_off.data_ptr(), big // 16, a, a2)  # noqa: E731
         elif case == "isum":
             keys = g.integers(0, big // 16, big).astype(np.uint64)
             res = ft.Array.init_scalar(big // 16)

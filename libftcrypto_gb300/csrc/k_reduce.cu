@@ -266,8 +266,8 @@ __global__ void __launch_bounds__(128, FT_SCAN_SUMS_MINB) k_scan_sums(ScanSet in
 }
 
 // rescan each thread's K points starting from its exclusive prefix ts[t]
-template <int K>
-__global__ void __launch_bounds__(128, FT_SCAN_APPLY_MINB) k_scan_apply(ScanSet io, size_t n, ScanSet ts, int exclusive)
+template <int K, int exclusive>
+__global__ void __launch_bounds__(128, FT_SCAN_APPLY_MINB) k_scan_apply(ScanSet io, size_t n, ScanSet ts)
 {
     uint4 *p = io.ptr();
     const size_t s = io.stride();
@@ -394,8 +394,10 @@ cudaError_t scan_set(const View *v, int m, size_t n, int exclusive, void *scratc
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if ((e = scan_set(ts, m, nt, 1, rest, st)) != cudaSuccess) return e;
-    if (K == 16) k_scan_apply<16><<<grid, 128, 0, st>>>(io, n, tset, exclusive);
-    else k_scan_apply<4><<<grid, 128, 0, st>>>(io, n, tset, exclusive);
+    if (K == 16 && exclusive) k_scan_apply<16, 1><<<grid, 128, 0, st>>>(io, n, tset);
+    else if (K == 16) k_scan_apply<16, 0><<<grid, 128, 0, st>>>(io, n, tset);
+    else if (exclusive) k_scan_apply<4, 1><<<grid, 128, 0, st>>>(io, n, tset);
+    else k_scan_apply<4, 0><<<grid, 128, 0, st>>>(io, n, tset);
     return cudaGetLastError();
 }
 
