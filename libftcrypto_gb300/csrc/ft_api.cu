@@ -157,22 +157,39 @@ cudaError_t d2h(void *dst, const void *src, size_t bytes, cudaStream_t st = null
     return cudaStreamSynchronize(st);
 }
 
-// Marks that the work just queued on the library stream completes a's
-// writes: an export of a that follows, with no other use of a in between,
-// waits for this point only (export_begin), not for everything queued after.
-cudaError_t mark_ready(ft_ge25519_array a)
+static cudaError_t record_on_stream(cudaEvent_t *ev)
 {
-    if (a->exposed.load()) return cudaSuccess;
-    if (!a->ready) {
-        cudaError_t e = cudaEventCreateWithFlags(&a->ready, cudaEventDisableTiming);
+    if (!*ev) {
+        cudaError_t e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
         if (e != cudaSuccess) {
-            a->ready = nullptr;
+            *ev = nullptr;
             return e;
         }
     }
+    return cudaEventRecord(*ev, g.stream);
+}
+
+// Marks that the work queued so far on the library stream has written a's
+// points [0, end), the first part of a write that mark_ready(a, end) then
+// completes: an export that follows copies that part while the rest is
+// computed.
+cudaError_t mark_part(ft_ge25519_array a)
+{
+    if (a->exposed.load()) return cudaSuccess;
+    return record_on_stream(&a->part);
+}
+
+// Marks that the work just queued on the library stream completes a's
+// writes: an export of a that follows, with no other use of a in between,
+// waits for this point only (export_begin), not for everything queued after.
+// part_end > 0: the call marked its first part [0, part_end) (mark_part).
+cudaError_t mark_ready(ft_ge25519_array a, size_t part_end = 0)
+{
+    if (a->exposed.load()) return cudaSuccess;
     const uint64_t t = a->touch.load();
-    const cudaError_t e = cudaEventRecord(a->ready, g.stream);
+    const cudaError_t e = record_on_stream(&a->ready);
     a->ready_touch = e == cudaSuccess ? t : UINT64_MAX; // a failed mark keeps exports in order
+    a->part_end = e == cudaSuccess ? part_end : 0;
     return e;
 }
 
@@ -184,8 +201,12 @@ cudaError_t mark_ready(ft_ge25519_array a)
 // scalar multiplication of c2).  Otherwise the library stream and its
 // scratch, in order.  The export buffer is only ever used on the transfer
 // stream, and every export ends with that stream synchronised.
-cudaError_t export_begin(const_ft_ge25519_array a, size_t bytes, void **buf, cudaStream_t *st)
+// *cut > 0: the marked call recorded its first part [0, *cut) (mark_part);
+// the transfer stream then waits for that part only, and the caller makes
+// it wait for the mark before it touches points from *cut on.
+cudaError_t export_begin(const_ft_ge25519_array a, size_t bytes, void **buf, cudaStream_t *st, size_t *cut)
 {
+    *cut = 0;
     const bool side = a->ready && !a->exposed.load() && a->touch.load() == a->ready_touch;
     if (!side) {
         *st = g.stream;
@@ -200,15 +221,42 @@ cudaError_t export_begin(const_ft_ge25519_array a, size_t bytes, void **buf, cud
         if ((e = cudaMallocFromPoolAsync(&g.xscratch, cap, g.pool, g.xfer)) != cudaSuccess) return e;
         g.xscratch_cap = cap;
     }
-    if ((e = cudaStreamWaitEvent(g.xfer, a->ready, 0)) != cudaSuccess) return e;
+    const bool parts = a->part && a->part_end > 0 && a->part_end < a->n;
+    if ((e = cudaStreamWaitEvent(g.xfer, parts ? a->part : a->ready, 0)) != cudaSuccess) return e;
     *buf = g.xscratch;
     *st = g.xfer;
+    *cut = parts ? a->part_end : 0;
     return cudaSuccess;
 }
 
-// the storage of a as a view, without counting a use (an export reads it on
-// the stream export_begin chose)
-View export_view(const_ft_ge25519_array a) { return View{a->planes, a->cap}; }
+// the storage of a from point `off` as a view, without counting a use (an
+// export reads it on the stream export_begin chose)
+View export_view(const_ft_ge25519_array a, size_t off = 0) { return View{a->planes + off, a->cap}; }
+
+// An export to host memory: conv(out, view, count, stream) writes bpp bytes
+// per point into the export buffer, which is copied to mem.  Where the call
+// that wrote a marked a first part, that part is converted and copied as
+// soon as it is written, then the rest after the mark.
+template <class Conv>
+ft_error export_to_host(uint8_t *mem, const_ft_ge25519_array a, size_t bpp, Conv conv)
+{
+    const size_t n = a->n;
+    void *s;
+    cudaStream_t st;
+    size_t cut;
+    CK(export_begin(a, align256(n * bpp), &s, &st, &cut));
+    size_t start = 0;
+    for (const size_t end : {cut, n}) {
+        if (end == start) continue;
+        if (start) CK(cudaStreamWaitEvent(st, a->ready, 0));
+        uint8_t *buf = (uint8_t *)s + start * bpp;
+        CK(conv(buf, export_view(a, start), end - start, st));
+        CK(cudaMemcpyAsync(mem + start * bpp, buf, (end - start) * bpp, cudaMemcpyDeviceToHost, st));
+        start = end;
+    }
+    CK(cudaStreamSynchronize(st));
+    return FT_ERR_NO_ERROR;
+}
 
 // Copies `bytes` of pinned host memory into one of two staging buffers on
 // the transfer stream, so that the copy overlaps kernels already queued on
@@ -684,12 +732,7 @@ ft_error ft_array_to_bytes_folded(uint8_t *mem, size_t n_bytes, const_ft_ge25519
     size_t n = array->n;
     if (n_bytes / FT_FOLDED_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
     if (n == 0) return FT_ERR_NO_ERROR;
-    void *s;
-    cudaStream_t st;
-    CK(export_begin(array, align256(n * 32), &s, &st));
-    CK(ft::encode((uint8_t *)s, export_view(array), n, st));
-    CK(d2h(mem, s, n * 32, st));
-    return FT_ERR_NO_ERROR;
+    return export_to_host(mem, array, 32, ft::encode);
 }
 
 ft_error ft_array_to_bytes_affine(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array array)
@@ -698,12 +741,7 @@ ft_error ft_array_to_bytes_affine(uint8_t *mem, size_t n_bytes, const_ft_ge25519
     size_t n = array->n;
     if (n_bytes / FT_AFFINE_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
     if (n == 0) return FT_ERR_NO_ERROR;
-    void *s;
-    cudaStream_t st;
-    CK(export_begin(array, align256(n * 64), &s, &st));
-    CK(ft::to_affine((uint8_t *)s, export_view(array), n, st));
-    CK(d2h(mem, s, n * 64, st));
-    return FT_ERR_NO_ERROR;
+    return export_to_host(mem, array, 64, ft::to_affine);
 }
 
 ft_error ft_array_to_bytes(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array array)
@@ -712,12 +750,7 @@ ft_error ft_array_to_bytes(uint8_t *mem, size_t n_bytes, const_ft_ge25519_array 
     size_t n = array->n;
     if (n_bytes / FT_EXTENDED_POINT_BYTES < n) return FT_ERR_INSUFFICIENT_SPACE;
     if (n == 0) return FT_ERR_NO_ERROR;
-    void *s;
-    cudaStream_t st;
-    CK(export_begin(array, align256(n * 160), &s, &st));
-    CK(ft::to_ref160((uint8_t *)s, export_view(array), n, st));
-    CK(d2h(mem, s, n * 160, st));
-    return FT_ERR_NO_ERROR;
+    return export_to_host(mem, array, 160, ft::to_ref160);
 }
 
 ft_error ft_array_from_bytes_folded(int64_t *res, ft_ge25519_array *array, const uint8_t *mem, size_t n_bytes)
@@ -810,8 +843,7 @@ void ft_array_free(ft_ge25519_array array)
 {
     if (!array) return;
     if (g.inited) dev_free(array->planes);
-    if (array->ready) cudaEventDestroy(array->ready);
-    delete array;
+    delete array; // destroys its events
 }
 
 size_t ft_array_get_length(const_ft_ge25519_array array) { return array->n; }
@@ -982,9 +1014,22 @@ ft_error ft_mul(ft_ge25519_array array, const uint8_t *scalars, size_t n)
         CK(h2d(p, scalars, n * 32));
         s = p;
     }
-    CK(ft::smul_var(ft::view_of(array), n, (const uint8_t *)s, 1, g.stream));
+    // Four or more waves of the ladder launch: all whole waves but the last
+    // in one launch, then the rest, marked as two parts, so that an export
+    // of the products (as the host-fed caller's next call usually is)
+    // converts and copies the first part while the last wave computes.
+    // Cut at a wave boundary, the two launches take as many waves as one.
+    const size_t wave = ft::ladder_wave_points();
+    const size_t cut = wave && n >= 4 * wave ? (n - 1) / wave * wave : 0;
+    if (cut) {
+        CK(ft::smul_var(ft::view_of(array), cut, (const uint8_t *)s, 1, g.stream));
+        CK(mark_part(array));
+        CK(ft::smul_var(ft::view_of(array, cut), n - cut, (const uint8_t *)s + cut * 32, 1, g.stream));
+    } else {
+        CK(ft::smul_var(ft::view_of(array), n, (const uint8_t *)s, 1, g.stream));
+    }
     if (sg) CK(cudaEventRecord(sg->consumed, g.stream));
-    CK(mark_ready(array));
+    CK(mark_ready(array, cut));
     if (sg) CK(cudaEventSynchronize(sg->copied)); // the caller may reuse its buffer
     return FT_ERR_NO_ERROR;
 }
@@ -1104,12 +1149,7 @@ ft_error ftx_array_to_packed(uint8_t *mem, size_t n_bytes, const_ft_ge25519_arra
     size_t n = array->n;
     if (n_bytes / 128 < n) return FT_ERR_INSUFFICIENT_SPACE;
     if (n == 0) return FT_ERR_NO_ERROR;
-    void *s;
-    cudaStream_t st;
-    CK(export_begin(array, align256(n * 128), &s, &st));
-    CK(ft::to_packed((uint8_t *)s, export_view(array), n, st));
-    CK(d2h(mem, s, n * 128, st));
-    return FT_ERR_NO_ERROR;
+    return export_to_host(mem, array, 128, ft::to_packed);
 }
 
 ft_error ftx_array_from_packed(ft_ge25519_array *array, const uint8_t *mem, size_t n_bytes)

@@ -26,11 +26,23 @@ struct ft_ge25519_array_s {
     // it (mark_ready), and stays valid while `touch` equals `ready_touch`.
     // `exposed`: the device address was handed out (ftx_array_device_view),
     // so writes the library does not see may follow and exports stay in
-    // stream order.
+    // stream order.  `part` (valid with `ready`, when `part_end` > 0): an
+    // event recorded after the marked call had written points [0, part_end),
+    // so an export can copy that part while the rest is computed.
     mutable std::atomic<uint64_t> touch{0};
     cudaEvent_t ready = nullptr;
     uint64_t ready_touch = 0;
+    cudaEvent_t part = nullptr;
+    size_t part_end = 0;
     mutable std::atomic<bool> exposed{false};
+    ft_ge25519_array_s() = default;
+    ft_ge25519_array_s(const ft_ge25519_array_s &) = delete;
+    ft_ge25519_array_s &operator=(const ft_ge25519_array_s &) = delete;
+    ~ft_ge25519_array_s()
+    {
+        if (ready) cudaEventDestroy(ready);
+        if (part) cudaEventDestroy(part);
+    }
 };
 
 namespace ft {
@@ -126,8 +138,16 @@ cudaError_t ladder_launch_192(uint4 *p, size_t s, size_t n, const uint4 *sc, int
 cudaError_t ladder_launch_224(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
 cudaError_t ladder_launch_384(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
 cudaError_t ladder_launch_448(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st);
+size_t ladder_wave_384();
+size_t ladder_wave_448();
+size_t ladder_wave_128();
+size_t ladder_wave_192();
+size_t ladder_wave_224();
 int ladder_block();
 int set_ladder_block(int nt);
+// points one wave of the current ladder launch holds (resident blocks x
+// threads), 0 if unknown
+size_t ladder_wave_points();
 
 // ---- reductions (k_reduce.cu)
 size_t reduce_scratch_bytes(size_t n);

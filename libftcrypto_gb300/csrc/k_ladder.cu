@@ -20,4 +20,6 @@ cudaError_t FT_CAT(ladder_launch_, FT_LADDER_NT)(uint4 *p, size_t s, size_t n, c
     return launch_ladder<FT_LADDER_NT>(p, s, n, sc, sc_step, st);
 }
 
+size_t FT_CAT(ladder_wave_, FT_LADDER_NT)() { return ladder_wave<FT_LADDER_NT>(); }
+
 } // namespace ft

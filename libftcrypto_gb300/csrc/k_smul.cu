@@ -19,6 +19,17 @@ int set_ladder_block(int nt)
     return 0;
 }
 
+size_t ladder_wave_points()
+{
+    switch (g_ladder_nt) {
+    case 128: return ladder_wave_128();
+    case 192: return ladder_wave_192();
+    case 224: return ladder_wave_224();
+    case 448: return ladder_wave_448();
+    default: return ladder_wave_384();
+    }
+}
+
 cudaError_t smul_var(View v, size_t n, const uint8_t *sc, int sc_step, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;

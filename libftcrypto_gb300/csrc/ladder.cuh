@@ -92,18 +92,47 @@ __global__ void __maxnreg__(tm_max_regs<NT>()) k_smul_var_tm(uint4 *p, size_t s,
 }
 
 template <int NT>
+const void *ladder_fn()
+{
+    if constexpr (NT > 256) return (const void *)k_smul_var_tm<NT>;
+    else return (const void *)k_smul_var<NT>;
+}
+
+template <int NT>
+inline SmemAttr ladder_attr;
+
+template <int NT>
 cudaError_t launch_ladder(uint4 *p, size_t s, size_t n, const uint4 *sc, int sc_step, cudaStream_t st)
 {
-    const void *fn;
-    if constexpr (NT > 256) fn = (const void *)k_smul_var_tm<NT>;
-    else fn = (const void *)k_smul_var<NT>;
-    static SmemAttr attr;
-    cudaError_t e = ensure_smem_attr(attr, fn, ladder_smem_bytes<NT>());
+    cudaError_t e = ensure_smem_attr(ladder_attr<NT>, ladder_fn<NT>(), ladder_smem_bytes<NT>());
     if (e != cudaSuccess) return e;
     unsigned grid = (unsigned)((n + NT - 1) / NT);
     if constexpr (NT > 256) k_smul_var_tm<NT><<<grid, NT, ladder_smem_bytes<NT>(), st>>>(p, s, n, sc, sc_step);
     else k_smul_var<NT><<<grid, NT, ladder_smem_bytes<NT>(), st>>>(p, s, n, sc, sc_step);
     return cudaGetLastError();
+}
+
+// points one wave of the launch holds: resident blocks per SM (from the
+// occupancy calculator) x SMs x NT; 0 if the calculator fails
+template <int NT>
+size_t ladder_wave()
+{
+    static std::atomic<size_t> known{0};
+    if (const size_t w = known.load(std::memory_order_relaxed)) return w;
+    if (ensure_smem_attr(ladder_attr<NT>, ladder_fn<NT>(), ladder_smem_bytes<NT>()) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ladder_fn<NT>(), NT, ladder_smem_bytes<NT>()) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    const size_t w = (size_t)per_sm * (size_t)sm_count() * NT;
+    known.store(w, std::memory_order_relaxed);
+    return w;
 }
 
 } // namespace ft

@@ -202,3 +202,40 @@ def test_length_changes_after_mark(ft, orc):
     one = ft.Array.from_packed(p[:1])
     one.mul(pinned(torch, k[:1]))
     assert (raw(ft, one, torch) == orc.to_ref160(orc.mul(p[:1], k[:1]))).all()
+
+
+@pytest.mark.parametrize("n", [291840, 300001])
+def test_mul_in_two_parts_then_exports(ft, orc, n):
+    """ft_mul over four or more waves of the ladder launch runs as two
+    launches (every whole wave but the last, then the rest), marked as two
+    parts, and its exports copy the first part while the second computes.
+    291,840 points are five whole waves at 152 SMs x 384 threads (the cut on
+    a wave boundary, a full last part), 300,001 cut inside the last wave.
+    Every format equals the oracle, with a second multiplication queued
+    behind, for pinned and pageable scalars, and after the length shrank
+    (past the cut: a shorter second part; below it: the export waits for
+    the whole call)."""
+    torch = pytest.importorskip("torch")
+    g = synth.rng(80 + n % 7)
+    p = ft.Array.from_scalars(synth.scalars_mod_L(g, n)).to_packed()
+    k = synth.scalars_mod_L(g, n)
+    w = orc.mul(p, k, threads=16)
+    c, c2 = ft.Array.from_packed(p), ft.Array.from_packed(p)
+    hk = pinned(torch, k)
+    c.mul(hk)
+    c2.mul(hk)
+    assert (raw(ft, c, torch) == orc.to_ref160(w)).all()
+    assert (c.to_bytes_folded() == orc.encode(w, 16)).all()
+    assert (c.to_bytes_affine() == orc.to_affine(w)).all()
+    assert (c.to_packed() == w).all()
+    assert (c2.to_packed() == w).all()
+    c3 = ft.Array.from_packed(p)
+    c3.mul(k)
+    assert (raw(ft, c3) == orc.to_ref160(w)).all()
+    # shorter, without a reallocation (above half the length): still past
+    # the cut, then below it
+    for m in (n - 5000, int(n * 0.6)):
+        c4 = ft.Array.from_packed(p)
+        c4.mul(hk)
+        c4.set_length(m)
+        assert (c4.to_bytes_folded() == orc.encode(w[:m], 16)).all()
