@@ -62,6 +62,9 @@ struct Ctx {
     };
     Stage stage[2];
     int stage_next = 0;
+    // ftx_encrypt's input copies: the first part's on the library stream,
+    // the rest's on the transfer stream
+    cudaEvent_t in_ev[2] = {nullptr, nullptr};
 };
 
 Ctx g;
@@ -352,15 +355,6 @@ ft_error with_new_array(ft_ge25519_array *out, size_t n, F fill)
     return FT_ERR_NO_ERROR;
 }
 
-// the OR of n words: a branch-free loop the compiler vectorises (an
-// early-exit scan of 1,048,576 plaintexts cost more than its copy)
-uint64_t or_all(const uint64_t *v, size_t n)
-{
-    uint64_t acc = 0;
-    for (size_t i = 0; i < n; ++i) acc |= v[i];
-    return acc;
-}
-
 ft_error check_idxs(const size_t *idxs, size_t n, size_t bound)
 {
     for (size_t i = 0; i < n; ++i)
@@ -512,6 +506,7 @@ ft_error init_device(int dev)
     int prio_lo = 0, prio_hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
     CK(cudaStreamCreateWithPriority(&g.xfer, cudaStreamNonBlocking, prio_hi));
+    for (auto &ev : g.in_ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     cudaMemPoolProps pp;
     std::memset(&pp, 0, sizeof pp);
     pp.allocType = cudaMemAllocationTypePinned;
@@ -550,6 +545,8 @@ void init_release()
         if (sg.copied) cudaEventDestroy(sg.copied);
         if (sg.consumed) cudaEventDestroy(sg.consumed);
     }
+    for (auto &ev : g.in_ev)
+        if (ev) cudaEventDestroy(ev);
     if (g.pool) cudaMemPoolDestroy(g.pool); // releases its memory once nothing is outstanding
     if (g.xfer) cudaStreamDestroy(g.xfer);
     if (g.stream) cudaStreamDestroy(g.stream);
@@ -1193,6 +1190,52 @@ ft_error ftx_encrypt_device(ft_ge25519_array c1, ft_ge25519_array c2, const uint
     return FT_ERR_NO_ERROR;
 }
 
+// The encryption of host inputs into new arrays a, b.  The inputs go over
+// in two parts: the first, one pass of the encryption grid, on the library
+// stream, which encrypts it while the transfer stream copies the rest; then
+// the rest is encrypted.  The plaintext bound is checked on the device (an
+// OR of all m after the copies), and the call returns once the inputs are
+// copied and checked, with the encryption still running.  Split at one pass,
+// the two launches take as many passes as one.  FT_ERR_BAD_SIZE if some
+// m_i >= 2^bits (the arrays' contents are then undefined).
+static ft_error encrypt_from_host(ft_ge25519_array a, ft_ge25519_array b, const uint64_t *m, const uint8_t *r,
+                                  size_t n, unsigned bits, const uint32_t *tab)
+{
+    if (n == 0) return FT_ERR_NO_ERROR;
+    void *s;
+    const size_t br = align256(n * 32), bm = align256(n * 8);
+    CK(scratch(&s, br + bm + 256));
+    uint8_t *dr = (uint8_t *)s;
+    uint64_t *dm = (uint64_t *)(dr + br), *dacc = (uint64_t *)(dr + br + bm);
+    const size_t first = std::min(n, ft::encrypt_pass());
+    const int mdig = m_digits(bits);
+    CK(cudaMemcpyAsync(dr, r, first * 32, cudaMemcpyHostToDevice, g.stream));
+    CK(cudaMemcpyAsync(dm, m, first * 8, cudaMemcpyHostToDevice, g.stream));
+    CK(cudaEventRecord(g.in_ev[0], g.stream)); // the first part is copied (and the scratch free)
+    CK(cudaStreamWaitEvent(g.xfer, g.in_ev[0], 0));
+    if (n > first) {
+        CK(cudaMemcpyAsync(dr + first * 32, r + first * 32, (n - first) * 32, cudaMemcpyHostToDevice, g.xfer));
+        CK(cudaMemcpyAsync(dm + first, m + first, (n - first) * 8, cudaMemcpyHostToDevice, g.xfer));
+        CK(cudaEventRecord(g.in_ev[1], g.xfer));
+    }
+    CK(ft::encrypt(ft::view_of(a), ft::view_of(b), first, dr, dm, mdig, tab, g.stream));
+    if (n > first) {
+        CK(cudaStreamWaitEvent(g.stream, g.in_ev[1], 0));
+        CK(ft::encrypt(ft::view_of(a, first), ft::view_of(b, first), n - first, dr + first * 32, dm + first, mdig,
+                       tab, g.stream));
+    }
+    CK(mark_ready(a));
+    CK(mark_ready(b));
+    uint64_t acc = 0;
+    if (bits < 64) {
+        CK(ft::or_words(dacc, dm, n, g.xfer));
+        CK(cudaMemcpyAsync(&acc, dacc, sizeof acc, cudaMemcpyDeviceToHost, g.xfer));
+    }
+    // the caller may reuse its buffers: both parts are copied
+    CK(cudaStreamSynchronize(g.xfer));
+    return bits < 64 && (acc >> bits) ? FT_ERR_BAD_SIZE : FT_ERR_NO_ERROR;
+}
+
 ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *pk, const uint64_t *m,
                      const uint8_t *r, size_t n, unsigned bits)
 {
@@ -1203,32 +1246,17 @@ ft_error ftx_encrypt(ft_ge25519_array *c1, ft_ge25519_array *c2, const uint8_t *
     const uint32_t *tab;
     ft_error err = ensure_pk_table(pk, &tab);
     if (err) return err;
-    // both inputs are queued, the plaintext bound is checked on the host
-    // while pinned inputs are in flight, and one wait covers both
-    void *s;
-    size_t br = align256(n * 32);
-    CK(scratch(&s, br + align256(n * 8)));
-    if (n) {
-        CK(cudaMemcpyAsync(s, r, n * 32, cudaMemcpyHostToDevice, g.stream));
-        CK(cudaMemcpyAsync((uint8_t *)s + br, m, n * 8, cudaMemcpyHostToDevice, g.stream));
-    }
-    const bool bad = bits < 64 && (or_all(m, n) >> bits);
-    if (n && (host_is_pinned(r) || host_is_pinned(m))) CK(cudaStreamSynchronize(g.stream));
-    if (bad) return FT_ERR_BAD_SIZE;
     ft_ge25519_array a, b;
     if ((err = arr_new(&a, n))) return err;
     if ((err = arr_new(&b, n))) {
         ft_array_free(a);
         return err;
     }
-    cudaError_t e = ft::encrypt(ft::view_of(a), ft::view_of(b), n, (const uint8_t *)s,
-                                (const uint64_t *)((uint8_t *)s + br), m_digits(bits), tab, g.stream);
-    if (e == cudaSuccess) e = mark_ready(a);
-    if (e == cudaSuccess) e = mark_ready(b);
-    if (e != cudaSuccess) {
-        ft_array_free(a);
+    const ft_error res = encrypt_from_host(a, b, m, r, n, bits, tab);
+    if (res) {
+        ft_array_free(a); // stream-ordered: after any launch that writes it
         ft_array_free(b);
-        return map_err(e);
+        return res;
     }
     *c1 = a;
     *c2 = b;

@@ -75,6 +75,8 @@ inline View view_of(const ft_ge25519_array_s *a, size_t off = 0)
 
 // ---- element-wise (k_elem.cu)
 cudaError_t set_zero(View v, size_t n, cudaStream_t st);
+// *acc = OR of v[0 .. n)
+cudaError_t or_words(uint64_t *acc, const uint64_t *v, size_t n, cudaStream_t st);
 cudaError_t broadcast(View dst, size_t n, View src, cudaStream_t st);
 cudaError_t add(View res, View src, size_t n, int sub, cudaStream_t st);
 // (r1, r2) +/-= (a1, a2) in one launch
@@ -113,6 +115,8 @@ constexpr size_t ENC_TABLES_BYTES = 2 * ENC_TABLE_WORDS * 4;
 // the table of the point at element 0 of q
 cudaError_t build_enc_table(uint32_t *d_table, View q, cudaStream_t st);
 // c1 = r*B, c2 = m*B + r*PK
+// ciphertexts one pass of the encryption grid takes (separate arrays)
+size_t encrypt_pass();
 cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *d_r, const uint64_t *d_m,
                     int m_digits, const uint32_t *d_tables, cudaStream_t st);
 // (c1, c2) += (r*B, r*PK): a fresh encryption of zero added in place

@@ -534,6 +534,16 @@ __global__ void __launch_bounds__(128) k_validate(const uint4 *p, size_t s, size
 
 // ------------------------------------------------------------ launchers
 
+// *acc |= OR of v[0 .. n): one 64-bit atomic per warp
+__global__ void __launch_bounds__(256) k_or_words(unsigned long long *acc, const uint64_t *v, size_t n)
+{
+    uint64_t x = 0;
+    FT_GRID_LOOP(i, n) x |= v[i];
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) x |= __shfl_xor_sync(0xffffffffu, x, d);
+    if ((threadIdx.x & 31) == 0 && x) atomicOr(acc, (unsigned long long)x);
+}
+
 #define FT_LAUNCH(kern, n, block, ...)                                  \
     do {                                                                 \
         if ((n) == 0) return cudaSuccess;                                \
@@ -542,6 +552,13 @@ __global__ void __launch_bounds__(128) k_validate(const uint4 *p, size_t s, size
     } while (0)
 
 cudaError_t set_zero(View v, size_t n, cudaStream_t st) { FT_LAUNCH(k_set_zero, n, 256, v.p, v.s, n); }
+
+cudaError_t or_words(uint64_t *acc, const uint64_t *v, size_t n, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(acc, 0, sizeof(uint64_t), st);
+    if (e != cudaSuccess) return e;
+    FT_LAUNCH(k_or_words, n, 256, (unsigned long long *)acc, v, n);
+}
 cudaError_t broadcast(View d, size_t n, View q, cudaStream_t st) { FT_LAUNCH(k_broadcast, n, 256, d.p, d.s, n, q.p, q.s); }
 cudaError_t add(View r, View a, size_t n, int sub, cudaStream_t st) { FT_LAUNCH(k_add, n, 128, r.p, r.s, a.p, a.s, n, sub); }
 cudaError_t add_ct(View r1, View r2, View a1, View a2, size_t n, int sub, cudaStream_t st)

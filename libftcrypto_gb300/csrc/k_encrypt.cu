@@ -185,6 +185,8 @@ static cudaError_t encrypt_launch(View c1, View c2, size_t n, const uint8_t *r, 
     return cudaGetLastError();
 }
 
+size_t encrypt_pass() { return (size_t)sm_count() * ENC_NT / (FT_ENC_SPLIT ? 2 : 1); }
+
 cudaError_t encrypt(View c1, View c2, size_t n, const uint8_t *r, const uint64_t *m, int mdig,
                     const uint32_t *tables, cudaStream_t st)
 {

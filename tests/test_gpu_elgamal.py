@@ -187,3 +187,52 @@ def test_encrypt_and_rerandomise_halves(ft, orc, n):
     want = orc.add(orc.add(before, orc.from_scalars(r2, threads=8), threads=8),
                    orc.mul(np.repeat(pk_packed, n, axis=0), r2, threads=8), threads=8)
     assert (c.to_bytes_folded() == orc.encode(want, 8)).all()
+
+
+@pytest.mark.parametrize("n", [1, 38912, 100001])
+def test_encrypt_host_inputs_in_two_parts(ft, orc, n):
+    """ftx_encrypt copies its host inputs in two parts (the first, one pass of
+    the encryption grid — 38,912 ciphertexts at 152 SMs — encrypted while the
+    rest is copied) and checks the plaintext bound on the device.  The points
+    equal ftx_encrypt_device's on the same inputs, from pinned and from
+    pageable buffers, and the oracle's on a sample; a plaintext at 2^bits in
+    the first part, the middle or the last element fails the call with
+    FT_ERR_BAD_SIZE; with 64-bit plaintexts nothing is rejected."""
+    torch = pytest.importorskip("torch")
+    g = synth.rng(170 + n)
+    sk, pk, pk_packed = keys(ft, g)
+    m = g.integers(0, 1 << 12, size=n, dtype=np.uint64)
+    r = synth.scalars_mod_L(g, n)
+
+    def on_device(mm, bits):
+        d_m, d_r = torch.from_numpy(mm.view(np.int64)).cuda(), torch.from_numpy(r).cuda()
+        torch.cuda.synchronize()
+        w1, w2 = ft.Array.init_scalar(n), ft.Array.init_scalar(n)
+        ft.encrypt_device(w1, w2, pk, d_m.data_ptr(), d_r.data_ptr(), n, bits)
+        return w1.to_bytes_folded(), w2.to_bytes_folded()
+
+    want1, want2 = on_device(m, 12)
+    idx = np.unique(np.concatenate([[0, n - 1], g.integers(0, n, 64)]))
+    rs = r[idx]
+    rB = orc.from_scalars(rs, threads=8)
+    c2_want = orc.add(orc.mul(np.repeat(pk_packed, len(idx), axis=0), rs, threads=8),
+                      orc.from_scalars(orc.small_to_scalars(m[idx]), threads=8), threads=8)
+    assert (want1[idx] == orc.encode(rB)).all()
+    assert (want2[idx] == orc.encode(c2_want)).all()
+    hm_t = torch.from_numpy(m.view(np.int64)).pin_memory()
+    hr_t = torch.from_numpy(r).pin_memory()
+    for mm, rr in ((hm_t.numpy().view(np.uint64), hr_t.numpy()), (m, r)):
+        c1, c2 = ft.encrypt(pk, mm, rr, 12)
+        assert (c1.to_bytes_folded() == want1).all()
+        assert (c2.to_bytes_folded() == want2).all()
+    for pos in sorted({0, n // 2, n - 1}):
+        bad = m.copy()
+        bad[pos] = 1 << 12
+        with pytest.raises(ft.FtError) as e:
+            ft.encrypt(pk, bad, r, 12)
+        assert e.value.code == 3
+    big = m | np.uint64(1 << 63)
+    w1, w2 = on_device(big, 64)
+    c1, c2 = ft.encrypt(pk, big, r, 64)
+    assert (c1.to_bytes_folded() == w1).all()
+    assert (c2.to_bytes_folded() == w2).all()
