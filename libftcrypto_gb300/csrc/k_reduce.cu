@@ -206,6 +206,9 @@ static int wave_fit_k(size_t n, int m, const int *ks, int nk, const int *residen
     return best;
 }
 
+// (An L1 prefetch of the thread's next pair of points before each step
+// measured slower: the two-half scan of 4,194,304 points 1.93 -> 1.96 ms,
+// the segmented sum of 16,777,216 points 1.66 -> 1.77 ms.)
 #ifndef FT_WALK_PAIRS
 #define FT_WALK_PAIRS 1
 #endif
