@@ -517,6 +517,24 @@ def test_ct_segmented_sum_both_halves(ft, orc, n, nseg):
     assert e.value.code == 2
 
 
+def test_ct_segmented_sum_without_points(ft, orc):
+    """Empty halves: every segment empty (the identity in both outputs, over
+    whatever they held), and no segments at all (nothing written)."""
+    torch = pytest.importorskip("torch")
+    d_off = torch.zeros(4, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    g = synth.rng(19)
+    o1, o2 = upload(ft, rand_points(orc, g, 3)), upload(ft, rand_points(orc, g, 3))
+    e1, e2 = ft.Array.init_scalar(0), ft.Array.init_scalar(0)
+    ft.ct_segmented_sum_csr_device(o1, o2, d_off.data_ptr(), 3, e1, e2)
+    ident = ft.Array.init_scalar(3).to_bytes_folded()
+    assert (o1.to_bytes_folded() == ident).all()
+    assert (o2.to_bytes_folded() == ident).all()
+    z1, z2 = ft.Array.init_scalar(0), ft.Array.init_scalar(0)
+    ft.ct_segmented_sum_csr_device(z1, z2, d_off.data_ptr(), 0, e1, e2)
+    assert len(z1) == 0 and len(z2) == 0
+
+
 @pytest.mark.parametrize("n", [1, 2, 1000, 1 << 20])
 def test_reduce_isum_all_keys_equal(ft, orc, n):
     """Every key the same (one segment of n points, a full reduction) and
