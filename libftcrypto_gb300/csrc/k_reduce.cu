@@ -213,7 +213,11 @@ static int wave_fit_k(size_t n, int m, const int *ks, int nk, const int *residen
 
 // (An L1 prefetch of the thread's next pair of points before each step
 // measured slower: the two-half scan of 4,194,304 points 1.93 -> 1.96 ms,
-// the segmented sum of 16,777,216 points 1.66 -> 1.77 ms.)
+// the segmented sum of 16,777,216 points 1.66 -> 1.77 ms.  Copying the
+// rescan's next pair into shared memory with cp.async while the current
+// pair is added — no registers held for it, 64 KB per block, still three
+// blocks per SM — measured the same for both halves, 1.046 -> 1.062 ms for
+// one array and 1.014 -> 1.064 ms for the prescan.)
 #ifndef FT_WALK_PAIRS
 #define FT_WALK_PAIRS 1
 #endif
