@@ -9,7 +9,10 @@ on the same inputs.
   encrypt + mult   1,048,576 ciphertexts of 8-bit plaintexts, then both
                    halves times a per-element secret scalar mod L: all
                    2,097,152 output points (ft_mul, ftcrypto.cu:986-1011;
-                   the oracle encrypts in the reference's composition)
+                   the oracle encrypts in the reference's composition).
+                   Host inputs, as in the end-to-end step: the encryption
+                   and each ladder run in two launches and the exports
+                   copy the first part while the second computes
   reductions       the sum of 16,777,216 ciphertexts (ft_array_reduce,
                    ftcrypto.cu:1414-1471), the segmented sum of the same
                    points into 1,048,576 CSR segments (ftcrypto.cu:1113-1217),
